@@ -1,0 +1,492 @@
+#!/usr/bin/env python
+"""Wilson Dslash benchmark: 4D, 32^3x64, FP32, 18-real links (the reference ABI).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one application of the hopping term to one checkerboard
+(1,048,576 output sites), cycling isign = +1/-1 and cb = 0/1.  Prints ONE JSON
+line on rank 0:
+
+  value       GFLOP/s of the device-resident kernel (1320 flop/site), inputs
+              resident in HBM; the gauge field (576 MiB) and spinors (2 x 96 MiB)
+              exceed the 129 MB L2, so no flush is needed between steps
+  e2e         the same metric through the drop-in C ABI (sse_su3dslash_wilson
+              of libgbdslash32.so) on pinned host arrays: host->device copy of
+              u and psi, the kernels and the device->host copy of res, every step
+  roofline    HBM bytes of the Dslash kernel (768 B/site compulsory) per launch
+              over its CUDA-event time, against MEASURED_PEAKS.json
+  cpu_baseline the oracle's table-driven port (OpenMP) on the host cores, on a
+              bounded slice of the same workload
+  variants    recon-12, FP64 and the 3D operator on 24^3x48 (not the headline)
+
+--impl reference times the CPU implementation of the path on the host cores:
+the reference library built from its own sources (oracle/_ref) where it was
+built for this host, else the oracle's port of it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+DIMS = (32, 32, 32, 64)
+DIMS_3D = (24, 24, 24, 48)
+FLOPS_4D, FLOPS_3D = 1320, 984
+WORKLOAD = "wilson_dslash_4d_32x32x32x64_f32_recon18"
+METRIC = "Dslash GFLOP/s at 32^3x64 (FP32, 4D, 18-real links, 1320 flop/site)"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.marks = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception as e:  # no nvidia-smi: report without clocks
+            log("clock sampler unavailable:", e)
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append((time.time(), ln.strip()))
+
+    def mark(self, what):
+        self.marks.append((what, time.time()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ts, ln in self.lines:
+            if not (t0 - 0.15 <= ts <= t1 + 0.15):
+                continue
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# Synthetic inputs on the device (random SU(3) links, N(0,1) spinors)
+# ---------------------------------------------------------------------------
+
+def su3_links(n, gen, torch):
+    """n random SU(3) matrices: Gaussian complex rows, Gram-Schmidt, row 2 =
+    conj(row0 x row1); returned packed as [n][j][i][2] (transposed), float64."""
+    out = torch.empty(n, 3, 3, 2, dtype=torch.float64, device="cuda")
+    chunk = 1 << 22
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        g = torch.randn(m, 2, 3, 2, dtype=torch.float64, device="cuda", generator=gen)
+        a = torch.view_as_complex(g)
+        r0 = a[:, 0] / a[:, 0].abs().pow(2).sum(-1, keepdim=True).sqrt()
+        r1 = a[:, 1] - (r0.conj() * a[:, 1]).sum(-1, keepdim=True) * r0
+        r1 = r1 / r1.abs().pow(2).sum(-1, keepdim=True).sqrt()
+        r2 = torch.linalg.cross(r0, r1).conj()
+        U = torch.stack([r0, r1, r2], dim=1)              # U[i][j]
+        out[s:s + m] = torch.view_as_real(U.transpose(1, 2).contiguous())  # [j][i]
+    return out
+
+
+def make_fields(dims, dtype, torch, seed=1234):
+    V = dims[0] * dims[1] * dims[2] * dims[3]
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    u = su3_links(V * 4, gen, torch).to(dtype).reshape(-1)
+    psi = torch.randn(V * 24, dtype=dtype, device="cuda", generator=gen)
+    return u, psi
+
+
+# ---------------------------------------------------------------------------
+# Timing helpers
+# ---------------------------------------------------------------------------
+
+def time_device(op, gauge, srcs, outs, steps, warmup, torch):
+    """Average ms per Dslash launch, CUDA events on the launching stream."""
+    stream = torch.cuda.current_stream()
+    combos = [(1, 0), (-1, 1), (-1, 0), (1, 1)]
+    for k in range(warmup):
+        isign, cb = combos[k % 4]
+        op.apply(gauge, srcs[cb], isign, cb, out=outs[1 - cb], stream=stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(steps):
+        isign, cb = combos[k % 4]
+        op.apply(gauge, srcs[cb], isign, cb, out=outs[1 - cb], stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None):
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    op = DslashOperator(dims, nd=nd, prec=prec, recon=recon)
+    dt = torch.float32 if prec == 32 else torch.float64
+    u, psi = fields if fields is not None else make_fields(dims, dt, torch)
+    gauge = op.pack_gauge(u)
+    srcs = [op.pack_spinor(psi, 0), op.pack_spinor(psi, 1)]
+    outs = [op.new_spinor(), op.new_spinor()]
+    ms = time_device(op, gauge, srcs, outs, steps, warmup, torch)
+    sites = op.volume_cb
+    res = {"ms": ms, "gflops": op.flops_per_site * sites / (ms * 1e6),
+           "gbs": op.bytes_per_site * sites / (ms * 1e6), "bytes_per_site": op.bytes_per_site,
+           "flops_per_site": op.flops_per_site, "sites": sites}
+    del gauge, srcs, outs
+    op.close()
+    return res
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload):
+    """Per-launch DRAM bytes of the Dslash kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"{workload}.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(float(ln.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU legs
+# ---------------------------------------------------------------------------
+
+def cpu_port_rate(u_host, psi_host, seconds, threads=None):
+    """GFLOP/s of the oracle's table-driven port on slices of the workload."""
+    import numpy as np
+    import oracle as O
+    lol = O.layout_table(O.LAYOUT_CB2, DIMS)
+    tabs = O.PortTables(4, DIMS, lol)
+    n = O.max_threads() if threads is None else threads
+    Vh = O.volume(DIMS) // 2
+    res = np.zeros_like(psi_host)
+    count = max(4096, Vh // 32)
+    tabs.apply_range(u_host, psi_host, res, 1, 0, 0, count, n)  # warm-up
+    done, first, t0 = 0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        tabs.apply_range(u_host, psi_host, res, 1, 0, first, count, n)
+        done += count
+        first = (first + count) % Vh
+    dt = time.perf_counter() - t0
+    tabs.close()
+    return FLOPS_4D * done / dt / 1e9, n, done, dt
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path on the host cores."""
+    import numpy as np
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle as O
+    V = O.volume(DIMS)
+    Vh = V // 2
+    rng = np.random.default_rng(1234)
+    log("reference arm: generating inputs")
+    u = O.random_gauge(rng, V).astype(np.float32)
+    psi = O.gaussian_spinor(rng, V).astype(np.float32)
+    res = np.zeros_like(psi)
+    kind = "port"
+    ref = None
+    if O.reference_available(32):
+        try:
+            ref = O.Reference(32)
+            ref.init(4, DIMS, O.LAYOUT_CB2)
+            kind = "reference"
+        except OSError:
+            ref = None
+    threads = O.max_threads()
+    if ref is not None:
+        # one full application per step (the reference has no sub-range entry)
+        def step(k):
+            ref.apply(4, u, psi, res, 1 if k % 2 == 0 else -1, k % 2)
+        count = Vh
+        sample = "full 32^3x64 FP32 applications through sse_su3dslash_wilson (reference built from its sources)"
+    else:
+        lol = O.layout_table(O.LAYOUT_CB2, DIMS)
+        tabs = O.PortTables(4, DIMS, lol)
+        t0 = time.perf_counter()
+        tabs.apply_range(u, psi, res, 1, 0, 0, Vh // 16, threads)
+        per_site = (time.perf_counter() - t0) / (Vh // 16)
+        budget = 60.0
+        count = int(min(Vh, max(4096, budget / max(1, args.steps + args.warmup) / per_site)))
+        state = {"first": 0}
+
+        def step(k):
+            tabs.apply_range(u, psi, res, 1 if k % 2 == 0 else -1, k % 2, state["first"], count, threads)
+            state["first"] = (state["first"] + count) % Vh
+        sample = f"{count} of {Vh} target sites per step (a slice of one 32^3x64 FP32 application), oracle port"
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(k)
+    dt = time.perf_counter() - t0
+    value = FLOPS_4D * count * args.steps / dt / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: random SU(3) links (Gram-Schmidt), N(0,1) spinors",
+            "config": {"workload": WORKLOAD, "lattice": list(DIMS), "nd": 4, "prec": 32, "recon": 18,
+                       "sites_per_step": count, "flops_per_site": FLOPS_4D},
+            "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build()
+    from sse_wilson_dslash_gb300 import _lib
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    from sse_wilson_dslash_gb300.legacy import SSEDslash
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # -- the headline: device-resident FP32 4D 32^3x64 recon 18 --------------
+    op = DslashOperator(DIMS, nd=4, prec=32, recon=18)
+    u, psi = make_fields(DIMS, torch.float32, torch)
+    gauge = op.pack_gauge(u)
+    srcs = [op.pack_spinor(psi, 0), op.pack_spinor(psi, 1)]
+    outs = [op.new_spinor(), op.new_spinor()]
+    stream = torch.cuda.current_stream()
+    combos = [(1, 0), (-1, 1), (-1, 0), (1, 1)]
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    gpu_index = int(vis.split(",")[local]) if vis and vis.split(",")[local].strip().isdigit() else local
+    clocks = ClockSampler(gpu_index)
+    clocks.start()
+    time.sleep(0.3)
+    for k in range(args.warmup):
+        isign, cb = combos[k % 4]
+        op.apply(gauge, srcs[cb], isign, cb, out=outs[1 - cb], stream=stream)
+    barrier()
+    launches0 = _lib.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_wall0 = time.time()
+    e0.record(stream)
+    for k in range(args.steps):
+        isign, cb = combos[k % 4]
+        op.apply(gauge, srcs[cb], isign, cb, out=outs[1 - cb], stream=stream)
+    e1.record(stream)
+    barrier()
+    t_wall1 = time.time()
+    launches = _lib.launch_count() - launches0
+    ms_total = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms = ms_total / args.steps
+    sites = op.volume_cb
+    value = FLOPS_4D * sites * args.steps * world / (ms_total * 1e6)
+    bytes_per_site = op.bytes_per_site
+    achieved = bytes_per_site * sites / (ms * 1e6)
+    # Keep the clock sampler running a little longer to cover short regions.
+    extra = time.time()
+    while time.time() - extra < 0.5:
+        for k in range(200):
+            isign, cb = combos[k % 4]
+            op.apply(gauge, srcs[cb], isign, cb, out=outs[1 - cb], stream=stream)
+        torch.cuda.synchronize()
+    t_wall1b = time.time()
+    clk = clocks.summary(t_wall0, t_wall1b)
+    clocks.stop()
+
+    peak, peak_kind = load_peaks()
+    traffic = profiled_traffic(WORKLOAD)
+
+    # -- e2e through the drop-in C ABI on pinned host memory ----------------
+    e2e = None
+    cpu = None
+    if True:  # every rank: replicas
+        u_h = torch.empty(u.numel(), dtype=torch.float32, pin_memory=True)
+        u_h.copy_(u.cpu())
+        psi_h = torch.empty(psi.numel(), dtype=torch.float32, pin_memory=True)
+        psi_h.copy_(psi.cpu())
+        res_h = torch.zeros(psi.numel(), dtype=torch.float32, pin_memory=True)
+        del gauge, srcs, outs
+        torch.cuda.empty_cache()
+        d = SSEDslash(32)
+        d.init_sse_su3dslash(DIMS, *_lib.canonical_callbacks(4, DIMS))
+        e2e_steps = max(5, min(args.steps, 50))
+        for k in range(max(2, min(args.warmup, 5))):
+            isign, cb = combos[k % 4]
+            d.sse_su3dslash_wilson(u_h, psi_h, res_h, isign, cb)
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            isign, cb = combos[k % 4]
+            d.sse_su3dslash_wilson(u_h, psi_h, res_h, isign, cb)
+        torch.cuda.synchronize()
+        barrier()
+        dt = time.perf_counter() - t0
+        e2e = {"value": FLOPS_4D * sites * e2e_steps * world / dt / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": op.volume * 72 * 4 + sites * 96, "d2h_bytes_per_step": sites * 96,
+               "steps": e2e_steps, "ms_per_step": dt / e2e_steps * 1e3,
+               "path": "sse_su3dslash_wilson (libgbdslash32.so), pinned host arrays, gauge copied every call"}
+        # gauge-resident variant: the caller promises u is unchanged between calls
+        from sse_wilson_dslash_gb300 import legacy
+        legacy.set_gauge_cache(True)
+        d.sse_su3dslash_wilson(u_h, psi_h, res_h, 1, 0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            isign, cb = combos[k % 4]
+            d.sse_su3dslash_wilson(u_h, psi_h, res_h, isign, cb)
+        dt = time.perf_counter() - t0
+        legacy.set_gauge_cache(False)
+        e2e["gauge_resident"] = {"value": FLOPS_4D * sites * e2e_steps * world / dt / 1e9,
+                                 "ms_per_step": dt / e2e_steps * 1e3,
+                                 "h2d_bytes_per_step": sites * 96, "d2h_bytes_per_step": sites * 96}
+        d.free_sse_su3dslash()
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            uh = u_h.numpy().reshape(-1, 4, 3, 3, 2)
+            ph = psi_h.numpy().reshape(-1, 4, 3, 2)
+            rate, n, done, secs = cpu_port_rate(uh, ph, args.cpu_seconds)
+            cpu = {"value": rate, "unit": "GFLOP/s", "cores": n, "kind": "port",
+                   "sample": f"{done} target sites ({done / sites:.2f} applications) of 32^3x64 FP32, "
+                             f"isign=+1 cb=0, oracle table-driven port, {secs:.1f} s"}
+        del u_h, psi_h, res_h
+
+    # -- variants (not the headline) -------------------------------------------
+    variants = {}
+    if not args.no_variants:
+        vsteps = max(20, min(args.steps, 200))
+        f32 = (u, psi)
+        variants["f32_recon12"] = device_variant(DIMS, 4, 32, 12, vsteps, 5, torch, fields=f32)
+        del f32
+        u64, psi64 = u.double(), psi.double()
+        del u, psi
+        torch.cuda.empty_cache()
+        variants["f64_recon18"] = device_variant(DIMS, 4, 64, 18, vsteps, 5, torch, fields=(u64, psi64))
+        variants["f64_recon12"] = device_variant(DIMS, 4, 64, 12, vsteps, 5, torch, fields=(u64, psi64))
+        del u64, psi64
+        torch.cuda.empty_cache()
+        variants["3d_24x24x24x48_f32_recon18"] = device_variant(DIMS_3D, 3, 32, 18, vsteps, 5, torch)
+        variants["3d_24x24x24x48_f32_recon12"] = device_variant(DIMS_3D, 3, 32, 12, vsteps, 5, torch)
+        for v in variants.values():
+            v["roofline_frac"] = v["gbs"] / peak
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic: random SU(3) links (Gaussian, Gram-Schmidt, row2 = conj(row0 x row1)), N(0,1) spinors",
+                "config": {"workload": WORKLOAD, "lattice": list(DIMS), "nd": 4, "prec": 32, "recon": 18,
+                           "sites_per_step": sites, "flops_per_site": FLOPS_4D, "bytes_per_site": bytes_per_site,
+                           "l2": "no flush: inputs (gauge 576 MiB, spinors 2 x 96 MiB) exceed the 129 MB L2",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "hbm_gbs": achieved,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_source": peak_kind,
+                             "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_site * sites,
+                             "kernel": "gbds::dslash_kernel<float,4,18,isign>"},
+                "gflops_ref_convention": 1390 * sites / (ms * 1e6),
+                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+                "variants": variants}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,204 @@
+/*
+ * gbdslash.h -- GB300-native Wilson Dslash: extended C ABI.
+ *
+ * The drop-in libraries libgbdslash32.so / libgbdslash64.so export the
+ * reference's own entry points (see sse_dslash.h and sse_dslash_3d.h in this
+ * directory).  This header is the layer underneath them, exported by
+ * libgbdslash.so:
+ *
+ *   1. precision-suffixed forms of every reference entry point
+ *      (gbds_sse_*_f32 / _f64), so FP32 and FP64 can be used in one process;
+ *   2. an operator handle that works on DEVICE pointers and CUDA streams, with
+ *      the fields held in the library's structure-of-arrays layout
+ *      (described below), optional 12-real gauge compression and status codes;
+ *   3. switches for the legacy host-pointer path.
+ *
+ * Everything is plain C: pointers, ints and sizes.  A CUDA stream is passed
+ * as `void*` (a cudaStream_t; NULL = the legacy default stream).
+ *
+ * Operator (identical to the reference, lib/sse_su3dslash_32bit_scalar.c:39-64):
+ *
+ *   res(x) = sum_{mu<nd} U_mu(x) (1 - isign g_mu) psi(x+mu)
+ *                      + U_mu(x-mu)^dag (1 + isign g_mu) psi(x-mu)
+ *
+ * on the sites x of checkerboard 1-cb, where cb is the checkerboard of the
+ * source, periodic boundaries, DeGrand-Rossi gamma matrices.  nd = 4 uses the
+ * 4D parity (x+y+z+t)&1; nd = 3 is the spatial operator with parity
+ * (x+y+z)&1 (lib/sse_su3dslash_32bit_scalar_3d.c).
+ *
+ * Internal layout (one checkerboard of a spinor, "SoA"):
+ *   site order within a checkerboard: nd=4: h = ((t*Lz+z)*Ly+y)*(Lx/2) + x/2
+ *                                     nd=3: h = t + Lt*(x/2 + (Lx/2)*(y+Ly*z))
+ *   FP32: 6 arrays of float4, array k holds reals 4k..4k+3 of the packed
+ *         spinor [4 spin][3 colour][2]; element (k, h) at k*stride + h.
+ *   FP64: 12 arrays of double2 (one complex each), element (k, h) at
+ *         k*stride + h.
+ *   stride = gbds_op_stride(): Vh rounded up to a multiple of 64.
+ * Gauge field (both checkerboards): block (p, mu) for p in {0,1}, mu < nd, at
+ *   offset (p*nd + mu) * C * stride elements, C components per link:
+ *   recon 18: 9 complex U_ij (i row, j column), component 3i+j;
+ *   recon 12: rows 0 and 1 only (6 complex); row 2 is rebuilt as
+ *             conj(row0 x row1) in the kernel (exact for SU(3) links).
+ *   FP32 uses float2 per complex for recon 18 and float4 pairs for recon 12;
+ *   FP64 uses double2 per complex.
+ */
+#ifndef GBDSLASH_H
+#define GBDSLASH_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBDS_VERSION_MAJOR 0
+#define GBDS_VERSION_MINOR 1
+
+/* Status codes returned by the extended API. */
+typedef enum gbds_status {
+    GBDS_SUCCESS = 0,
+    GBDS_ERROR_INVALID_VALUE = 1,   /* bad argument (dims, isign, cb, pointer, size) */
+    GBDS_ERROR_NOT_INITIALIZED = 2, /* handle or legacy state not set up            */
+    GBDS_ERROR_CUDA = 3,            /* a CUDA runtime call failed                   */
+    GBDS_ERROR_OUT_OF_MEMORY = 4,   /* device or pinned host allocation failed      */
+    GBDS_ERROR_UNSUPPORTED = 5      /* valid request this build does not implement  */
+} gbds_status;
+
+/* Storage precisions and gauge compressions. */
+#define GBDS_PREC_F32 32
+#define GBDS_PREC_F64 64
+#define GBDS_RECON_18 18
+#define GBDS_RECON_12 12
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char *gbds_get_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* Operator handle (device pointers)                                         */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gbds_op_s *gbds_op;
+
+/* Create an operator for lattice dims[4] = {Lx, Ly, Lz, Lt}.
+ * nd = 4: all four dims even; nd = 3: Lx, Ly, Lz even (Lt any >= 1).
+ * prec: GBDS_PREC_F32 or GBDS_PREC_F64.  recon: GBDS_RECON_18 or _12.
+ * Does not allocate device memory. */
+int gbds_op_create(gbds_op *op, const int dims[4], int nd, int prec, int recon);
+int gbds_op_destroy(gbds_op op);
+
+/* Caller site layout for pack/unpack: site_table[i] = caller linear index of
+ * internal site i (i = p*Vh + h, internal order above), n = V entries, a
+ * permutation of [0, V).  NULL (or the identity) selects the canonical
+ * layout, in which the caller's order equals the internal order (QDP++ cb2
+ * for nd = 4, cb3d for nd = 3).  Copies the table to the device. */
+int gbds_op_set_layout(gbds_op op, const int *site_table, int n);
+/* 1 if the operator uses the canonical layout (no permutation). */
+int gbds_op_is_canonical(gbds_op op);
+
+size_t gbds_op_spinor_bytes(gbds_op op); /* one checkerboard, internal layout */
+size_t gbds_op_gauge_bytes(gbds_op op);  /* both checkerboards                */
+int gbds_op_geometry(gbds_op op, int *volume, int *volume_cb, int *stride);
+
+/* Packed (reference layout) device arrays <-> internal layout.
+ *   u_packed:   [V][4][3][3][2] reals, u[s][mu][j][i] = U_mu(s)_ij, caller order
+ *   psi_packed: [V][4][3][2] reals, caller order (full lattice)
+ * pack_spinor reads the sites of checkerboard `parity`; unpack_spinor writes
+ * only those sites of psi_packed. */
+int gbds_op_pack_gauge(gbds_op op, const void *u_packed, void *gauge, void *stream);
+int gbds_op_pack_spinor(gbds_op op, const void *psi_packed, int parity, void *spinor, void *stream);
+int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity, void *psi_packed, void *stream);
+
+/* res (checkerboard 1-cb) = Dslash psi (checkerboard cb), internal layout.
+ * isign +1: D, -1: D^dagger; any other isign is a no-op (returns
+ * GBDS_SUCCESS), as in the reference.  cb must be 0 or 1. */
+int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
+                   int isign, int cb, void *stream);
+
+/* Threads per block of the Dslash launch (0 = library default).  Used by the
+ * autotuner; any multiple of 32 in [32, 1024]. */
+int gbds_op_set_block(gbds_op op, int threads);
+
+/* Number of kernels this library has launched in this process (all kinds). */
+long long gbds_kernel_launch_count(void);
+
+/* ------------------------------------------------------------------------ */
+/* Reference entry points with precision suffixes                            */
+/* ------------------------------------------------------------------------ */
+/* Same arguments and behaviour as init_sse_su3dslash & co.
+ * (include/sse_dslash.h:13-36, include/sse_dslash_3d.h:13-33 of the
+ * reference); u, psi and res are HOST pointers in the packed layout. */
+
+void gbds_sse_init_f32(const int *latt_size,
+                       void (*getSiteCoords)(int coord[], int node, int linearsite),
+                       int (*getLinearSiteIndex)(const int coord[]),
+                       int (*nodeNumber)(const int coord[]));
+void gbds_sse_free_f32(void);
+void gbds_sse_wilson_f32(float *u, float *psi, float *res, int isign, int cb);
+void gbds_sse_init_3d_f32(const int *latt_size,
+                          void (*getSiteCoords)(int coord[], int node, int linearsite),
+                          int (*getLinearSiteIndex)(const int coord[]),
+                          int (*nodeNumber)(const int coord[]));
+void gbds_sse_free_3d_f32(void);
+void gbds_sse_wilson_3d_f32(float *u, float *psi, float *res, int isign, int cb);
+void gbds_pack_gauge_field_f32(int volume, float *u, float *u_tmp);
+void gbds_unpack_gauge_field_f32(int volume, float *u_tmp, float *u);
+
+void gbds_sse_init_f64(const int *latt_size,
+                       void (*getSiteCoords)(int coord[], int node, int linearsite),
+                       int (*getLinearSiteIndex)(const int coord[]),
+                       int (*nodeNumber)(const int coord[]));
+void gbds_sse_free_f64(void);
+void gbds_sse_wilson_f64(double *u, double *psi, double *res, int isign, int cb);
+void gbds_sse_init_3d_f64(const int *latt_size,
+                          void (*getSiteCoords)(int coord[], int node, int linearsite),
+                          int (*getLinearSiteIndex)(const int coord[]),
+                          int (*nodeNumber)(const int coord[]));
+void gbds_sse_free_3d_f64(void);
+void gbds_sse_wilson_3d_f64(double *u, double *psi, double *res, int isign, int cb);
+void gbds_pack_gauge_field_f64(int volume, double *u, double *u_tmp);
+void gbds_unpack_gauge_field_f64(int volume, double *u_tmp, double *u);
+
+/* ------------------------------------------------------------------------ */
+/* QDP++ site-order callbacks                                                */
+/* ------------------------------------------------------------------------ */
+/* Ready-made getSiteCoords / getLinearSiteIndex / nodeNumber for callers of
+ * init_sse_su3dslash* that do not link QDP++: they describe the QDP++ cb2
+ * order (nd = 4) or cb3d order (nd = 3) of the lattice selected by
+ * gbds_layout_select (process-wide; select before the init call that uses
+ * them).  With these callbacks the drop-in runs without any permutation. */
+int gbds_layout_select(int nd, const int dims[4]);
+void gbds_layout_site_coords(int coord[], int node, int linearsite);
+int gbds_layout_linear_site_index(const int coord[]);
+int gbds_layout_node_number(const int coord[]);
+
+/* ------------------------------------------------------------------------ */
+/* Legacy host-pointer path: switches and state                              */
+/* ------------------------------------------------------------------------ */
+
+/* On an error in a legacy init (odd dimension, bad layout, allocation
+ * failure) the reference prints to stderr and calls exit(1)
+ * (lib/sse_su3dslash_32bit_scalar.c:103-110).  That is the default here too;
+ * set 0 to print and return instead, leaving the library uninitialised. */
+int gbds_legacy_set_exit_on_error(int on);
+
+/* Gauge residency: with 1, a legacy apply whose `u` pointer equals the
+ * previous call's skips the host->device copy and repacking of the gauge
+ * field.  The caller promises not to change the contents behind that pointer
+ * until gbds_legacy_invalidate_gauge() is called.  Default 0 (every call
+ * reads `u`, like the reference). */
+int gbds_legacy_set_gauge_cache(int on);
+int gbds_legacy_invalidate_gauge(void);
+
+/* Gauge compression used by the legacy path (18 = exact copy of the links;
+ * 12 = two rows, third rebuilt; only valid for SU(3) links).  Default 18.
+ * Takes effect at the next init. */
+int gbds_legacy_set_recon(int recon);
+
+/* Refcount of a legacy context: prec 32/64, nd 4/3 (0 = not initialised). */
+int gbds_legacy_refcount(int prec, int nd);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBDSLASH_H */

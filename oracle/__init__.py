@@ -62,6 +62,10 @@ def lib() -> ctypes.CDLL:
     L.orc_tables_free.argtypes = [ctypes.c_void_p]
     L.orc_dslash_port_f32.argtypes = [ctypes.c_void_p, f32p, f32p, f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.orc_dslash_port_f64.argtypes = [ctypes.c_void_p, f64p, f64p, f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.orc_dslash_port_range_f32.argtypes = [ctypes.c_void_p, f32p, f32p, f32p, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.orc_dslash_port_range_f64.argtypes = [ctypes.c_void_p, f64p, f64p, f64p, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.orc_max_threads.restype = ctypes.c_int
     _lib = L
     return L
@@ -306,6 +310,14 @@ class PortTables:
         else:
             lib().orc_dslash_port_f64(self._h, _ptr(u, ctypes.c_double), _ptr(psi, ctypes.c_double),
                                       _ptr(res, ctypes.c_double), int(isign), int(cb), int(n))
+
+    def apply_range(self, u, psi, res, isign: int, cb: int, first: int, count: int,
+                    nthreads: int | None = None) -> None:
+        """Only target sites [first, first+count) in traversal order."""
+        n = max_threads() if nthreads is None else nthreads
+        f = lib().orc_dslash_port_range_f32 if res.dtype == np.float32 else lib().orc_dslash_port_range_f64
+        ct = ctypes.c_float if res.dtype == np.float32 else ctypes.c_double
+        f(self._h, _ptr(u, ct), _ptr(psi, ct), _ptr(res, ct), int(isign), int(cb), int(first), int(count), int(n))
 
     def close(self):
         if self._h:

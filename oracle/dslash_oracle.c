@@ -390,12 +390,18 @@ static void NAME##_hop(NAME##_c acc[4][3], const REAL *psi_site, const REAL *lin
         acc[3][c].re += r3.re;      acc[3][c].im += r3.im;                           \
     }                                                                                \
 }                                                                                    \
-void orc_dslash_port_##NAME(const orc_tables *t, const REAL *u, const REAL *psi,     \
-                            REAL *res, int isign, int cb, int nthreads)              \
+/* Target sites [first, first+count) of checkerboard 1-cb, in traversal order  \
+ * (a bounded slice of one application, for timing on the host).  */               \
+void orc_dslash_port_range_##NAME(const orc_tables *t, const REAL *u,                \
+                                  const REAL *psi, REAL *res, int isign, int cb,     \
+                                  int first, int count, int nthreads)                \
 {                                                                                    \
     if (isign != 1 && isign != -1) return;                                           \
+    if (first < 0) first = 0;                                                        \
+    if (count > t->Vh - first) count = t->Vh - first;                                \
+    if (count <= 0) return;                                                          \
     int target = 1 - cb;                                                             \
-    int lo = target * t->Vh, hi = lo + t->Vh;                                        \
+    int lo = target * t->Vh + first, hi = lo + count;                                \
     int nd = t->nd;                                                                  \
     if (nthreads <= 0) nthreads = 1;                                                 \
     _Pragma("omp parallel for schedule(static) num_threads(nthreads)")               \
@@ -412,6 +418,11 @@ void orc_dslash_port_##NAME(const orc_tables *t, const REAL *u, const REAL *psi,
         }                                                                            \
         memcpy(res + (size_t)site * 24, acc, sizeof(acc));                           \
     }                                                                                \
+}                                                                                    \
+void orc_dslash_port_##NAME(const orc_tables *t, const REAL *u, const REAL *psi,     \
+                            REAL *res, int isign, int cb, int nthreads)              \
+{                                                                                    \
+    orc_dslash_port_range_##NAME(t, u, psi, res, isign, cb, 0, t->Vh, nthreads);     \
 }
 
 /* Spin projection (1 - sigma*gamma_mu) psi for sigma = +1, in half-spinor form:

@@ -1,0 +1,9 @@
+// FP64 instantiations of the fused Dslash kernel (4D/3D x recon 18/12 x isign).
+#include "dslash_kernel.cuh"
+
+namespace gbds {
+cudaError_t launch_dslash_f64(const Geom &g, int recon, const void *gauge, const void *psi, void *res,
+                              int isign, int cb, int block, cudaStream_t stream) {
+    return launch_dslash_t<double>(g, recon, gauge, psi, res, isign, cb, block, stream);
+}
+}  // namespace gbds

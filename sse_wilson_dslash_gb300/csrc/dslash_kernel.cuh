@@ -1,0 +1,340 @@
+// Fused Wilson Dslash kernel: gather + spin projection + SU(3) multiply +
+// reconstruction + accumulation over all 2*nd hops of one output site, in
+// registers, in one pass.
+//
+// Replaces, on the device, the reference's per-site SSE kernels
+// (lib/site_dslash_32bit_scalar.c:23-3098, lib/site_dslash_64bit_scalar.c:20-4926),
+// its decomp / decomp_hvv / mvv_recons / recons stage kernels
+// (lib/decomp_32bit_parscalar.c, lib/decomp_hvv_32bit_parscalar.c,
+// lib/mvv_recons_32bit_parscalar.c, lib/recons_32bit_parscalar.c) and its
+// neighbour tables (lib/shift_tables_scalar.c:191-313): neighbours are
+// computed from the site index with periodic wrap-around.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gbds_internal.h"
+
+namespace gbds {
+
+template <typename T>
+struct cx {
+    T r, i;
+};
+
+// Multiply by a coefficient in {+1, -1, +i, -i} (codes 0, 1, 2, 3).
+template <int CODE, typename T>
+__device__ __forceinline__ cx<T> mulc(cx<T> a) {
+    if constexpr (CODE == 0) return a;
+    else if constexpr (CODE == 1) return {-a.r, -a.i};
+    else if constexpr (CODE == 2) return {-a.i, a.r};
+    else return {a.i, -a.r};
+}
+
+template <typename T>
+__device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return {a.r + b.r, a.i + b.i}; }
+
+// Half-spinor form of (1 - sigma*gamma_mu), DeGrand-Rossi basis, sigma = +1:
+//   h0 = psi0 + a0*psi[j0], h1 = psi1 + a1*psi[j1]
+//   after the colour multiply w = M h:  lower spin components r2 = b2*w[k2],
+//   r3 = b3*w[k3].  sigma = -1 flips every coefficient (code ^ 1).
+// mu=0: h0=psi0-i psi3, h1=psi1-i psi2; r2= i w1, r3= i w0
+// mu=1: h0=psi0+psi3,   h1=psi1-psi2;   r2=-w1,   r3= w0
+// mu=2: h0=psi0-i psi2, h1=psi1+i psi3; r2= i w0, r3=-i w1
+// mu=3: h0=psi0-psi2,   h1=psi1-psi3;   r2=-w0,   r3=-w1
+template <int MU> struct Proj;
+template <> struct Proj<0> { static constexpr int j0 = 3, a0 = 3, j1 = 2, a1 = 3, k2 = 1, b2 = 2, k3 = 0, b3 = 2; };
+template <> struct Proj<1> { static constexpr int j0 = 3, a0 = 0, j1 = 2, a1 = 1, k2 = 1, b2 = 1, k3 = 0, b3 = 0; };
+template <> struct Proj<2> { static constexpr int j0 = 2, a0 = 3, j1 = 3, a1 = 2, k2 = 0, b2 = 2, k3 = 1, b3 = 3; };
+template <> struct Proj<3> { static constexpr int j0 = 2, a0 = 1, j1 = 3, a1 = 1, k2 = 0, b2 = 1, k3 = 1, b3 = 1; };
+
+template <int MU, int SIGMA, typename T>
+__device__ __forceinline__ void project(const cx<T> (&s)[4][3], cx<T> (&h)[2][3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIGMA > 0 ? 0 : 1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        h[0][c] = cadd(s[0][c], mulc<P::a0 ^ f>(s[P::j0][c]));
+        h[1][c] = cadd(s[1][c], mulc<P::a1 ^ f>(s[P::j1][c]));
+    }
+}
+
+template <int MU, int SIGMA, typename T>
+__device__ __forceinline__ void reconstruct(cx<T> (&acc)[4][3], const cx<T> (&w)[2][3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIGMA > 0 ? 0 : 1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        acc[0][c] = cadd(acc[0][c], w[0][c]);
+        acc[1][c] = cadd(acc[1][c], w[1][c]);
+        acc[2][c] = cadd(acc[2][c], mulc<P::b2 ^ f>(w[P::k2][c]));
+        acc[3][c] = cadd(acc[3][c], mulc<P::b3 ^ f>(w[P::k3][c]));
+    }
+}
+
+// w_k = U h_k  (DAG = false) or U^dagger h_k (DAG = true), k = 0, 1.
+template <bool DAG, typename T>
+__device__ __forceinline__ void su3_mul(const cx<T> (&U)[3][3], const cx<T> (&h)[2][3], cx<T> (&w)[2][3]) {
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            T re = 0, im = 0;
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const cx<T> m = DAG ? U[j][i] : U[i][j];
+                const cx<T> v = h[k][j];
+                if (DAG) {
+                    re = fma(m.r, v.r, re); re = fma(m.i, v.i, re);
+                    im = fma(m.r, v.i, im); im = fma(-m.i, v.r, im);
+                } else {
+                    re = fma(m.r, v.r, re); re = fma(-m.i, v.i, re);
+                    im = fma(m.r, v.i, im); im = fma(m.i, v.r, im);
+                }
+            }
+            w[k][i] = {re, im};
+        }
+    }
+}
+
+// Third row of an SU(3) matrix from the first two: row2 = conj(row0 x row1).
+template <typename T>
+__device__ __forceinline__ void reconstruct_row2(cx<T> (&U)[3][3]) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const int k = (j + 1) % 3, l = (j + 2) % 3;
+        // (a x b)_j = a_k b_l - a_l b_k
+        const cx<T> a = U[0][k], b = U[1][l], c = U[0][l], d = U[1][k];
+        T re = a.r * b.r - a.i * b.i - (c.r * d.r - c.i * d.i);
+        T im = a.r * b.i + a.i * b.r - (c.r * d.i + c.i * d.r);
+        U[2][j] = {re, -im};
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Field access (structure-of-arrays, see gbdslash.h)
+// ---------------------------------------------------------------------------
+
+template <typename T> struct Field;
+
+template <>
+struct Field<float> {
+    static constexpr int SPINOR_VECS = 6;  // float4
+    __device__ __forceinline__ static void load_spinor(const float4 *__restrict__ p, int stride, int h,
+                                                       cx<float> (&s)[4][3]) {
+        float v[24];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            float4 q = __ldg(p + k * stride + h);
+            v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+        }
+#pragma unroll
+        for (int sp = 0; sp < 4; sp++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) s[sp][c] = {v[(sp * 3 + c) * 2], v[(sp * 3 + c) * 2 + 1]};
+    }
+    __device__ __forceinline__ static void store_spinor(float4 *__restrict__ p, int stride, int h,
+                                                        const cx<float> (&s)[4][3]) {
+        float v[24];
+#pragma unroll
+        for (int sp = 0; sp < 4; sp++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) { v[(sp * 3 + c) * 2] = s[sp][c].r; v[(sp * 3 + c) * 2 + 1] = s[sp][c].i; }
+#pragma unroll
+        for (int k = 0; k < 6; k++) __stcs(p + k * stride + h, make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
+    }
+    // Link block base: vector elements per link for a recon.
+    static constexpr int link_vecs(int recon) { return recon == 18 ? 9 : 3; }
+    template <int RECON>
+    __device__ __forceinline__ static void load_link(const void *__restrict__ base, int stride, int h,
+                                                     cx<float> (&U)[3][3]) {
+        if constexpr (RECON == 18) {
+            const float2 *p = static_cast<const float2 *>(base);
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                float2 q = __ldg(p + k * stride + h);
+                U[k / 3][k % 3] = {q.x, q.y};
+            }
+        } else {
+            const float4 *p = static_cast<const float4 *>(base);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                float4 q = __ldg(p + k * stride + h);
+                U[(2 * k) / 3][(2 * k) % 3] = {q.x, q.y};
+                U[(2 * k + 1) / 3][(2 * k + 1) % 3] = {q.z, q.w};
+            }
+            reconstruct_row2(U);
+        }
+    }
+};
+
+template <>
+struct Field<double> {
+    static constexpr int SPINOR_VECS = 12;  // double2
+    __device__ __forceinline__ static void load_spinor(const double2 *__restrict__ p, int stride, int h,
+                                                       cx<double> (&s)[4][3]) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+            double2 q = __ldg(p + k * stride + h);
+            s[k / 3][k % 3] = {q.x, q.y};
+        }
+    }
+    __device__ __forceinline__ static void store_spinor(double2 *__restrict__ p, int stride, int h,
+                                                        const cx<double> (&s)[4][3]) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) __stcs(p + k * stride + h, make_double2(s[k / 3][k % 3].r, s[k / 3][k % 3].i));
+    }
+    static constexpr int link_vecs(int recon) { return recon == 18 ? 9 : 6; }
+    template <int RECON>
+    __device__ __forceinline__ static void load_link(const void *__restrict__ base, int stride, int h,
+                                                     cx<double> (&U)[3][3]) {
+        const double2 *p = static_cast<const double2 *>(base);
+        constexpr int n = RECON == 18 ? 9 : 6;
+#pragma unroll
+        for (int k = 0; k < n; k++) {
+            double2 q = __ldg(p + k * stride + h);
+            U[k / 3][k % 3] = {q.x, q.y};
+        }
+        if constexpr (RECON == 12) reconstruct_row2(U);
+    }
+};
+
+template <typename T> struct VecOf;
+template <> struct VecOf<float> { using S = float4; using G = float2; static constexpr int GB = 8; };
+template <> struct VecOf<double> { using S = double2; using G = double2; static constexpr int GB = 16; };
+
+// Bytes of one gauge vector element (float2 / float4 / double2) per recon.
+template <typename T, int RECON>
+constexpr int gauge_vec_bytes() {
+    return sizeof(T) == 4 ? (RECON == 18 ? 8 : 16) : 16;
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour indexing (periodic), internal site order of gbdslash.h
+// ---------------------------------------------------------------------------
+
+struct Nbr {
+    int f[4], b[4];  // source-checkerboard index of x+mu / x-mu
+};
+
+template <int ND>
+__device__ __forceinline__ void neighbours(const Geom &g, int h, int pt, Nbr &n) {
+    const int Lxh = g.Lxh;
+    if constexpr (ND == 4) {
+        int r = h;
+        const int xh = r % Lxh; r /= Lxh;
+        const int y = r % g.L[1]; r /= g.L[1];
+        const int z = r % g.L[2];
+        const int t = r / g.L[2];
+        const int x = 2 * xh + ((y + z + t + pt) & 1);
+        const int row = h - xh;
+        const int xp = (x + 1 == g.L[0]) ? 0 : x + 1;
+        const int xm = (x == 0) ? g.L[0] - 1 : x - 1;
+        n.f[0] = row + (xp >> 1);
+        n.b[0] = row + (xm >> 1);
+        const int sy = Lxh, sz = Lxh * g.L[1], st = sz * g.L[2];
+        n.f[1] = (y + 1 == g.L[1]) ? h - (g.L[1] - 1) * sy : h + sy;
+        n.b[1] = (y == 0) ? h + (g.L[1] - 1) * sy : h - sy;
+        n.f[2] = (z + 1 == g.L[2]) ? h - (g.L[2] - 1) * sz : h + sz;
+        n.b[2] = (z == 0) ? h + (g.L[2] - 1) * sz : h - sz;
+        n.f[3] = (t + 1 == g.L[3]) ? h - (g.L[3] - 1) * st : h + st;
+        n.b[3] = (t == 0) ? h + (g.L[3] - 1) * st : h - st;
+    } else {
+        const int Lt = g.L[3];
+        int r = h / Lt;
+        const int xh = r % Lxh; r /= Lxh;
+        const int y = r % g.L[1];
+        const int z = r / g.L[1];
+        const int x = 2 * xh + ((y + z + pt) & 1);
+        const int row = h - xh * Lt;
+        const int xp = (x + 1 == g.L[0]) ? 0 : x + 1;
+        const int xm = (x == 0) ? g.L[0] - 1 : x - 1;
+        n.f[0] = row + (xp >> 1) * Lt;
+        n.b[0] = row + (xm >> 1) * Lt;
+        const int sy = Lt * Lxh, sz = sy * g.L[1];
+        n.f[1] = (y + 1 == g.L[1]) ? h - (g.L[1] - 1) * sy : h + sy;
+        n.b[1] = (y == 0) ? h + (g.L[1] - 1) * sy : h - sy;
+        n.f[2] = (z + 1 == g.L[2]) ? h - (g.L[2] - 1) * sz : h + sz;
+        n.b[2] = (z == 0) ? h + (g.L[2] - 1) * sz : h - sz;
+        n.f[3] = n.b[3] = h;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The kernel
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct DslashArgs {
+    Geom g;
+    const typename VecOf<T>::S *psi;  // source checkerboard (cb)
+    typename VecOf<T>::S *res;        // target checkerboard (1-cb)
+    const char *gauge;                // both checkerboards
+    size_t link_block_bytes;          // bytes of one (parity, mu) block
+    int pt;                           // target parity = 1 - cb
+};
+
+template <typename T, int ND, int RECON, int ISIGN, int MU>
+__device__ __forceinline__ void hop_pair(const DslashArgs<T> &a, int h, const Nbr &n, cx<T> (&acc)[4][3]) {
+    using F = Field<T>;
+    const int ps = 1 - a.pt;
+    cx<T> s[4][3], hs[2][3], w[2][3], U[3][3];
+    // forward: U_mu(x) (1 - isign gamma_mu) psi(x + mu)
+    F::load_spinor(a.psi, a.g.stride, n.f[MU], s);
+    F::template load_link<RECON>(a.gauge + (size_t)(a.pt * ND + MU) * a.link_block_bytes, a.g.stride, h, U);
+    project<MU, ISIGN>(s, hs);
+    su3_mul<false>(U, hs, w);
+    reconstruct<MU, ISIGN>(acc, w);
+    // backward: U_mu(x - mu)^dagger (1 + isign gamma_mu) psi(x - mu)
+    F::load_spinor(a.psi, a.g.stride, n.b[MU], s);
+    F::template load_link<RECON>(a.gauge + (size_t)(ps * ND + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
+    project<MU, -ISIGN>(s, hs);
+    su3_mul<true>(U, hs, w);
+    reconstruct<MU, -ISIGN>(acc, w);
+}
+
+template <typename T, int ND, int RECON, int ISIGN>
+__global__ void __launch_bounds__(256) dslash_kernel(const DslashArgs<T> a) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= a.g.Vh) return;
+    Nbr n;
+    neighbours<ND>(a.g, h, a.pt, n);
+    cx<T> acc[4][3];
+#pragma unroll
+    for (int s = 0; s < 4; s++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) acc[s][c] = {T(0), T(0)};
+    hop_pair<T, ND, RECON, ISIGN, 0>(a, h, n, acc);
+    hop_pair<T, ND, RECON, ISIGN, 1>(a, h, n, acc);
+    hop_pair<T, ND, RECON, ISIGN, 2>(a, h, n, acc);
+    if constexpr (ND == 4) hop_pair<T, ND, RECON, ISIGN, 3>(a, h, n, acc);
+    Field<T>::store_spinor(a.res, a.g.stride, h, acc);
+}
+
+template <typename T>
+cudaError_t launch_dslash_t(const Geom &g, int recon, const void *gauge, const void *psi, void *res,
+                            int isign, int cb, int block, cudaStream_t stream) {
+    DslashArgs<T> a;
+    a.g = g;
+    a.psi = static_cast<const typename VecOf<T>::S *>(psi);
+    a.res = static_cast<typename VecOf<T>::S *>(res);
+    a.gauge = static_cast<const char *>(gauge);
+    const int vec_bytes = sizeof(T) == 4 ? (recon == 18 ? 8 : 16) : 16;
+    a.link_block_bytes = (size_t)Field<T>::link_vecs(recon) * g.stride * vec_bytes;
+    a.pt = 1 - cb;
+    if (block <= 0) block = 128;
+    const dim3 grid((g.Vh + block - 1) / block);
+#define GBDS_LAUNCH(ND, R, S) dslash_kernel<T, ND, R, S><<<grid, block, 0, stream>>>(a)
+    if (g.nd == 4) {
+        if (recon == 18) { if (isign > 0) GBDS_LAUNCH(4, 18, 1); else GBDS_LAUNCH(4, 18, -1); }
+        else             { if (isign > 0) GBDS_LAUNCH(4, 12, 1); else GBDS_LAUNCH(4, 12, -1); }
+    } else {
+        if (recon == 18) { if (isign > 0) GBDS_LAUNCH(3, 18, 1); else GBDS_LAUNCH(3, 18, -1); }
+        else             { if (isign > 0) GBDS_LAUNCH(3, 12, 1); else GBDS_LAUNCH(3, 12, -1); }
+    }
+#undef GBDS_LAUNCH
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace gbds

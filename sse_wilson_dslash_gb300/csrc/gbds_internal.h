@@ -1,0 +1,59 @@
+// Internal declarations shared by the translation units of libgbdslash.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "gbdslash.h"
+
+namespace gbds {
+
+// Lattice geometry as the kernels see it.
+struct Geom {
+    int L[4];     // Lx, Ly, Lz, Lt
+    int nd;       // 4 or 3
+    int Lxh;      // Lx / 2
+    int V;        // full volume
+    int Vh;       // sites per checkerboard
+    int stride;   // elements between consecutive components of a field
+};
+
+// Record an error message for gbds_get_last_error() and return `code`.
+int set_error(int code, const std::string &msg);
+int cuda_error(cudaError_t e, const char *where);
+void count_launch(int n = 1);
+
+// Launchers (defined in dslash_f32.cu / dslash_f64.cu / layout.cu).
+// All pointers are device pointers; `stream` is a cudaStream_t.
+cudaError_t launch_dslash_f32(const Geom &g, int recon, const void *gauge, const void *psi,
+                              void *res, int isign, int cb, int block, cudaStream_t stream);
+cudaError_t launch_dslash_f64(const Geom &g, int recon, const void *gauge, const void *psi,
+                              void *res, int isign, int cb, int block, cudaStream_t stream);
+
+// site0: first caller site held by the packed buffer (0 for a full lattice).
+cudaError_t launch_pack_spinor(const Geom &g, int prec, const void *psi_packed, const int *site_table,
+                               int site0, int parity, void *spinor, cudaStream_t stream);
+cudaError_t launch_unpack_spinor(const Geom &g, int prec, const void *spinor, const int *site_table,
+                                 int site0, int parity, void *psi_packed, cudaStream_t stream);
+cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_packed,
+                              const int *site_table, void *gauge, cudaStream_t stream);
+
+// Sizes in bytes of the internal fields.
+size_t spinor_bytes(const Geom &g, int prec);
+size_t gauge_bytes(const Geom &g, int prec, int recon);
+
+// Validate dims for an nd-dimensional operator and fill a Geom.
+int make_geom(const int dims[4], int nd, Geom *g);
+
+}  // namespace gbds
+
+struct gbds_op_s {
+    gbds::Geom g;
+    int prec;
+    int recon;
+    int block;
+    int *d_site_table;  // device copy of the layout table, or nullptr (canonical)
+};

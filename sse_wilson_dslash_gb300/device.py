@@ -1,0 +1,141 @@
+"""Device-resident Dslash on torch CUDA tensors, through the extended C ABI
+(``gbds_op_*`` in include/gbdslash.h).
+
+Torch is used only for device memory and streams; the work is done by the
+library's own kernels.  Fields in the internal layout are plain uint8 CUDA
+tensors of ``spinor_bytes`` / ``gauge_bytes``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+def _dptr(t) -> int:
+    if not t.is_cuda:
+        raise TypeError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise TypeError("expected a contiguous tensor")
+    return t.data_ptr()
+
+
+def _stream(stream):
+    import torch
+    s = torch.cuda.current_stream() if stream is None else stream
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class DslashOperator:
+    """Wilson hopping term on one lattice.
+
+    dims: (Lx, Ly, Lz, Lt); nd: 4 (4D, QDP++ cb2 order) or 3 (spatial, cb3d);
+    prec: 32 or 64; recon: 18 or 12 (12-real links, SU(3) only).
+    """
+
+    def __init__(self, dims, nd: int = 4, prec: int = 32, recon: int = 18, device=None):
+        import torch
+        self.dims = tuple(int(v) for v in dims)
+        self.nd, self.prec, self.recon = nd, prec, recon
+        self.device = torch.device("cuda" if device is None else device)
+        L = _lib.core()
+        h = ctypes.c_void_p()
+        d = (ctypes.c_int * 4)(*self.dims)
+        _lib.check(L.gbds_op_create(ctypes.byref(h), d, nd, prec, recon))
+        self._h = h
+        V, Vh, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(L.gbds_op_geometry(h, ctypes.byref(V), ctypes.byref(Vh), ctypes.byref(st)))
+        self.volume, self.volume_cb, self.stride = V.value, Vh.value, st.value
+        self.spinor_bytes = int(L.gbds_op_spinor_bytes(h))
+        self.gauge_bytes = int(L.gbds_op_gauge_bytes(h))
+        self.real_dtype = torch.float32 if prec == 32 else torch.float64
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.core().gbds_op_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- layout ----------------------------------------------------------------
+    def set_layout(self, site_table) -> None:
+        """Caller site order: ``site_table[i]`` = caller index of internal site i
+        (None = canonical)."""
+        if site_table is None:
+            _lib.check(_lib.core().gbds_op_set_layout(self._h, None, 0))
+            return
+        t = np.ascontiguousarray(site_table, dtype=np.int32)
+        _lib.check(_lib.core().gbds_op_set_layout(self._h, t.ctypes.data_as(_lib.c_int_p), int(t.size)))
+
+    @property
+    def canonical(self) -> bool:
+        return bool(_lib.core().gbds_op_is_canonical(self._h))
+
+    def set_block(self, threads: int) -> None:
+        _lib.check(_lib.core().gbds_op_set_block(self._h, int(threads)))
+
+    # -- fields ----------------------------------------------------------------
+    def new_spinor(self):
+        import torch
+        return torch.empty(self.spinor_bytes, dtype=torch.uint8, device=self.device)
+
+    def new_gauge(self):
+        import torch
+        return torch.empty(self.gauge_bytes, dtype=torch.uint8, device=self.device)
+
+    def pack_gauge(self, u_packed, out=None, stream=None):
+        """Packed device gauge ``[V][4][3][3][2]`` -> internal layout."""
+        out = self.new_gauge() if out is None else out
+        self._check_real(u_packed, self.volume * 72)
+        _lib.check(_lib.core().gbds_op_pack_gauge(self._h, ctypes.c_void_p(_dptr(u_packed)),
+                                                  ctypes.c_void_p(_dptr(out)), _stream(stream)))
+        return out
+
+    def pack_spinor(self, psi_packed, parity: int, out=None, stream=None):
+        """Packed device spinor ``[V][4][3][2]`` (checkerboard ``parity``) -> internal."""
+        out = self.new_spinor() if out is None else out
+        self._check_real(psi_packed, self.volume * 24)
+        _lib.check(_lib.core().gbds_op_pack_spinor(self._h, ctypes.c_void_p(_dptr(psi_packed)), int(parity),
+                                                   ctypes.c_void_p(_dptr(out)), _stream(stream)))
+        return out
+
+    def unpack_spinor(self, spinor, parity: int, psi_packed, stream=None):
+        """Internal spinor -> the checkerboard ``parity`` sites of a packed array."""
+        self._check_real(psi_packed, self.volume * 24)
+        _lib.check(_lib.core().gbds_op_unpack_spinor(self._h, ctypes.c_void_p(_dptr(spinor)), int(parity),
+                                                     ctypes.c_void_p(_dptr(psi_packed)), _stream(stream)))
+        return psi_packed
+
+    def apply(self, gauge, psi, isign: int, cb: int, out=None, stream=None):
+        """out (checkerboard 1-cb) = Dslash psi (checkerboard cb), internal layout."""
+        out = self.new_spinor() if out is None else out
+        for t, n in ((gauge, self.gauge_bytes), (psi, self.spinor_bytes), (out, self.spinor_bytes)):
+            if t.numel() * t.element_size() < n:
+                raise ValueError("field buffer too small")
+        _lib.check(_lib.core().gbds_op_dslash(self._h, ctypes.c_void_p(_dptr(gauge)), ctypes.c_void_p(_dptr(psi)),
+                                              ctypes.c_void_p(_dptr(out)), int(isign), int(cb), _stream(stream)))
+        return out
+
+    def _check_real(self, t, n):
+        if t.dtype != self.real_dtype:
+            raise TypeError(f"expected {self.real_dtype}")
+        if t.numel() < n:
+            raise ValueError("packed array too small")
+
+    # -- flop / byte accounting ----------------------------------------------------
+    @property
+    def flops_per_site(self) -> int:
+        """Standard count: 1320 (4D), 984 (3D) per output site."""
+        return 1320 if self.nd == 4 else 984
+
+    @property
+    def bytes_per_site(self) -> int:
+        """Compulsory HBM bytes per output site: 2 spinors + 2*nd links."""
+        real = 4 if self.prec == 32 else 8
+        return 2 * 24 * real + 2 * self.nd * self.recon * real

@@ -1,0 +1,201 @@
+"""The C-ABI libraries load and export every symbol the headers declare, and
+the host-side logic of the drop-in behaves like the reference.  CPU only: no
+call here launches a kernel."""
+import ctypes
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+INCLUDE = os.path.join(ROOT, "include")
+
+REFERENCE_API = ["init_sse_su3dslash", "free_sse_su3dslash", "sse_su3dslash_wilson",
+                 "sse_su3dslash_prepost_receives", "init_sse_su3dslash_3d", "free_sse_su3dslash_3d",
+                 "sse_su3dslash_wilson_3d", "pack_gauge_field", "unpack_gauge_field"]
+
+
+@pytest.fixture(scope="session")
+def libs():
+    from sse_wilson_dslash_gb300 import _build
+    return _build.build()
+
+
+def declared(header):
+    txt = open(os.path.join(INCLUDE, header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", txt)) - {"if", "while", "sizeof"})
+
+
+def exported(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True, check=True).stdout
+    return {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+
+
+def test_core_exports_everything_in_gbdslash_h(libs):
+    names = declared("gbdslash.h")
+    assert len(names) > 30
+    missing = set(names) - exported(libs["core"])
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+def test_dropin_exports_reference_api(libs, prec):
+    ex = exported(libs[f"legacy{prec}"])
+    decl = set(declared("sse_dslash.h")) | set(declared("sse_dslash_3d.h"))
+    assert decl == set(REFERENCE_API)
+    assert set(REFERENCE_API) <= ex
+    ctypes.CDLL(libs[f"legacy{prec}"])  # loads and resolves libgbdslash.so via $ORIGIN
+
+
+def test_op_create_validation(libs):
+    from sse_wilson_dslash_gb300 import _lib
+    L = _lib.core()
+    h = ctypes.c_void_p()
+    for dims, nd, prec, recon, ok in [((4, 4, 4, 4), 4, 32, 18, True), ((4, 4, 4, 3), 4, 32, 18, False),
+                                      ((4, 4, 4, 3), 3, 64, 12, True), ((3, 4, 4, 4), 3, 32, 18, False),
+                                      ((4, 4, 4, 4), 5, 32, 18, False), ((4, 4, 4, 4), 4, 16, 18, False),
+                                      ((4, 4, 4, 4), 4, 32, 9, False), ((0, 4, 4, 4), 4, 32, 18, False)]:
+        d = (ctypes.c_int * 4)(*dims)
+        rc = L.gbds_op_create(ctypes.byref(h), d, nd, prec, recon)
+        assert (rc == 0) == ok, (dims, nd, prec, recon, L.gbds_get_last_error())
+        if ok:
+            V, Vh, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            assert L.gbds_op_geometry(h, ctypes.byref(V), ctypes.byref(Vh), ctypes.byref(st)) == 0
+            assert V.value == np.prod(dims) and Vh.value * 2 == V.value and st.value % 64 == 0 and st.value >= Vh.value
+            real = prec // 8
+            assert L.gbds_op_spinor_bytes(h) == 24 * real * st.value
+            assert L.gbds_op_gauge_bytes(h) == 2 * nd * recon * real * st.value
+            assert L.gbds_op_set_block(h, 96) == 0 and L.gbds_op_set_block(h, 100) != 0
+            L.gbds_op_destroy(h)
+        else:
+            assert L.gbds_get_last_error()
+
+
+def test_set_layout_rejects_non_permutations(libs):
+    from sse_wilson_dslash_gb300 import _lib
+    L = _lib.core()
+    h = ctypes.c_void_p()
+    assert L.gbds_op_create(ctypes.byref(h), (ctypes.c_int * 4)(2, 2, 2, 2), 4, 32, 18) == 0
+    bad = np.zeros(16, np.int32)
+    assert L.gbds_op_set_layout(h, bad.ctypes.data_as(_lib.c_int_p), 16) == 1
+    short = np.arange(8, dtype=np.int32)
+    assert L.gbds_op_set_layout(h, short.ctypes.data_as(_lib.c_int_p), 8) == 1
+    ident = np.arange(16, dtype=np.int32)  # identity: canonical, no device copy needed
+    assert L.gbds_op_set_layout(h, ident.ctypes.data_as(_lib.c_int_p), 16) == 0
+    assert L.gbds_op_is_canonical(h) == 1
+    L.gbds_op_destroy(h)
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+def test_pack_gauge_field_matches_reference_semantics(libs, prec):
+    """pack_gauge_field: u[mu][cb][ix] -> u_tmp[cb][ix][mu] (lib/packer_nopad.c:29-45);
+    unpack_gauge_field copies index for index (lib/packer_nopad.c:47-69)."""
+    from sse_wilson_dslash_gb300.legacy import SSEDslash
+    d = SSEDslash(prec)
+    vol = 6
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((4, 2, vol, 3, 3, 2)).astype(d.dtype)
+    out = np.zeros((2, vol, 4, 3, 3, 2), d.dtype)
+    d.pack_gauge_field(vol, u, out)
+    assert np.array_equal(out, np.transpose(u, (1, 2, 0, 3, 4, 5)))
+    back = np.zeros_like(u)
+    d.unpack_gauge_field(vol, out, back)
+    assert np.array_equal(back.ravel(), out.ravel())
+    import oracle as O
+    if O.reference_available(prec):
+        R = O.Reference(prec)
+        ref = np.zeros_like(out)
+        rp = ctypes.POINTER(R.real)
+        R.L.pack_gauge_field(vol, u.ctypes.data_as(rp), ref.ctypes.data_as(rp))
+        assert np.array_equal(ref, out)
+        rb = np.zeros_like(u)
+        R.L.unpack_gauge_field(vol, out.ctypes.data_as(rp), rb.ctypes.data_as(rp))
+        assert np.array_equal(rb, back)
+
+
+def _child(code):
+    env = dict(os.environ, PYTHONPATH=ROOT, CUDA_VISIBLE_DEVICES="")
+    return subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=120)
+
+
+@pytest.mark.parametrize("prec,nd,dims,msg", [(32, 4, (4, 4, 3, 4), "latt_size[2]=3"),
+                                               (64, 4, (5, 4, 4, 4), "latt_size[0]=5"),
+                                               (32, 3, (4, 3, 4, 4), "latt_size[1]=3")])
+def test_init_with_odd_dims_exits_like_reference(libs, prec, nd, dims, msg):
+    code = f"""
+from sse_wilson_dslash_gb300.legacy import SSEDslash
+import oracle as O
+d = SSEDslash({prec})
+O.set_callback_layout(O.LAYOUT_LEX, {dims})
+gc, gl, nn = O.callbacks()
+d.{'init_sse_su3dslash' if nd == 4 else 'init_sse_su3dslash_3d'}({dims}, gc, gl, nn)
+print("not reached")
+"""
+    r = _child(code)
+    assert r.returncode == 1, r.stdout + r.stderr
+    assert msg in r.stderr and "not reached" not in r.stdout
+
+
+def test_init_odd_time_extent_is_fine_in_3d_validation(libs):
+    """3D checks only extents 0..2 (lib/sse_su3dslash_32bit_scalar_3d.c:95-102);
+    with exit disabled and no GPU the init fails later, at allocation."""
+    code = """
+from sse_wilson_dslash_gb300 import legacy
+import oracle as O
+legacy.set_exit_on_error(False)
+d = legacy.SSEDslash(32)
+O.set_callback_layout(O.LAYOUT_CB3D, (4, 4, 4, 3))
+gc, gl, nn = O.callbacks()
+d.init_sse_su3dslash_3d((4, 4, 4, 3), gc, gl, nn)
+print("calls", O.callback_calls(), "ref", legacy.refcount(32, 3))
+"""
+    r = _child(code)
+    assert r.returncode == 0, r.stderr
+    assert "odd" not in r.stderr and "even" not in r.stderr
+    # every site's index was read through the callbacks before allocation
+    assert "calls 384" in r.stdout, r.stdout
+
+
+def test_no_exit_mode_and_uninitialised_apply(libs):
+    code = """
+import numpy as np
+from sse_wilson_dslash_gb300 import legacy
+import oracle as O
+legacy.set_exit_on_error(False)
+d = legacy.SSEDslash(32)
+O.set_callback_layout(O.LAYOUT_LEX, (4, 4, 3, 4))
+gc, gl, nn = O.callbacks()
+d.init_sse_su3dslash((4, 4, 3, 4), gc, gl, nn)
+print("ref", legacy.refcount(32, 4))
+u = np.zeros((48, 4, 3, 3, 2), np.float32); p = np.zeros((48, 4, 3, 2), np.float32); r = p.copy()
+d.sse_su3dslash_wilson(u, p, r, 1, 0)      # not initialised: message, no crash
+d.sse_su3dslash_wilson(u, p, r, 7, 0)      # bad isign: silent no-op
+d.free_sse_su3dslash(); d.free_sse_su3dslash()   # free when uninitialised: no-op
+d.sse_su3dslash_prepost_receives()
+print("done")
+"""
+    r = _child(code)
+    assert r.returncode == 0, r.stderr
+    assert "ref 0" in r.stdout and "done" in r.stdout
+    assert "latt_size[2]=3" in r.stderr
+    assert r.stderr.count("called before init") == 1
+
+
+def test_bad_layout_callbacks_rejected(libs):
+    code = """
+from sse_wilson_dslash_gb300 import legacy
+legacy.set_exit_on_error(False)
+d = legacy.SSEDslash(64)
+d.init_sse_su3dslash((2, 2, 2, 2), None, lambda c: 0)
+print("ref", legacy.refcount(64, 4))
+d.init_sse_su3dslash((2, 2, 2, 2), lambda c, n, l: None, lambda c: c[0] + 2 * (c[1] + 2 * (c[2] + 2 * c[3])))
+print("ref", legacy.refcount(64, 4))
+"""
+    r = _child(code)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.count("ref 0") == 2
+    assert "one-to-one" in r.stderr and "not the inverse" in r.stderr
