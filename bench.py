@@ -377,7 +377,7 @@ def run_gb300(args):
     # -- e2e through the drop-in C ABI on pinned host memory ----------------
     e2e = None
     cpu = None
-    if True:  # every rank: replicas
+    if not args.no_e2e:  # every rank: replicas
         u_h = torch.empty(u.numel(), dtype=torch.float32, pin_memory=True)
         u_h.copy_(u.cpu())
         psi_h = torch.empty(psi.numel(), dtype=torch.float32, pin_memory=True)
@@ -424,7 +424,7 @@ def run_gb300(args):
             ph = psi_h.numpy().reshape(-1, 4, 3, 2)
             rate, n, done, secs = cpu_port_rate(uh, ph, args.cpu_seconds)
             cpu = {"value": rate, "unit": "GFLOP/s", "cores": n, "kind": "port",
-                   "sample": f"{done} target sites ({done / sites:.2f} applications) of 32^3x64 FP32, "
+                   "sample": f"{done} target sites ({done / sites:.2f} applications) of {'x'.join(map(str, DIMS))} FP32, "
                              f"isign=+1 cb=0, oracle table-driven port, {secs:.1f} s"}
         del u_h, psi_h, res_h
 
@@ -480,7 +480,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--dims", default=None,
+                    help="Lx,Ly,Lz,Lt of the 4D workload (default 32,32,32,64; smaller cases are for profiling)")
     args = ap.parse_args()
+    if args.dims:
+        global DIMS, WORKLOAD
+        DIMS = tuple(int(v) for v in args.dims.split(","))
+        WORKLOAD = "wilson_dslash_4d_%dx%dx%dx%d_f32_recon18" % DIMS
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
