@@ -122,6 +122,40 @@ int gbds_op_set_block(gbds_op op, int threads);
 long long gbds_kernel_launch_count(void);
 
 /* ------------------------------------------------------------------------ */
+/* Packed-layout Dslash that allocates nothing                               */
+/* ------------------------------------------------------------------------ */
+/* No counterpart in the reference.  For callers that must not allocate
+ * device memory themselves or have the library do it: code whose device
+ * memory belongs to a framework's own pool allocator, code running under a
+ * fixed device-memory budget, and latency-critical loops that cannot afford
+ * the device-wide synchronisation that cudaFree implies.  Such callers still
+ * need the operator on the reference's packed layout, which goes through
+ * structure-of-arrays copies of the gauge field and of both spinor
+ * checkerboards; here those copies live in one file-scope device array of
+ * GBDS_NOALLOC_SCRATCH_BYTES (12 MiB) that every GPU which loads this part of
+ * the library holds until the process exits.
+ *
+ *   u_packed, psi_packed, res_packed: DEVICE pointers, 16-byte aligned, in the
+ *     reference's packed layouts (u[V][4][3][3][2], psi/res[V][4][3][2]) and
+ *     the QDP++ site order (cb2 for nd = 4, cb3d for nd = 3).
+ *   Writes the sites of checkerboard 1-cb of res_packed, like
+ *   sse_su3dslash_wilson; isign other than +1/-1 does nothing.
+ *   Lattices above GBDS_NOALLOC_MAX_SITES sites are rejected with
+ *   GBDS_ERROR_INVALID_VALUE.  No cudaMalloc, cudaFree or other allocating
+ *   call is made.
+ *   The first call on each device looks up that device's address of the
+ *   array (cudaGetSymbolAddress) with the device current; make that first call
+ *   before any stream capture.
+ *   All calls share the array and it keeps the last call's contents (every
+ *   element a call reads it has written first).  Calls that overlap on the
+ *   GPU -- different streams, or different host threads -- race on it: issue
+ *   them in order on one stream. */
+#define GBDS_NOALLOC_MAX_SITES 32768
+#define GBDS_NOALLOC_SCRATCH_BYTES 12582912
+int gbds_dslash_packed_noalloc_f32(const int dims[4], int nd, const float *u_packed, const float *psi_packed,
+                                   float *res_packed, int isign, int cb, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Reference entry points with precision suffixes                            */
 /* ------------------------------------------------------------------------ */
 /* Same arguments and behaviour as init_sse_su3dslash & co.
