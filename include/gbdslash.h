@@ -114,9 +114,13 @@ int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity, void *psi_
 int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
                    int isign, int cb, void *stream);
 
-/* Threads per block of the Dslash launch (0 = library default).  Used by the
- * autotuner; any multiple of 32 in [32, 1024]. */
-int gbds_op_set_block(gbds_op op, int threads);
+/* Launch tuning of gbds_op_dslash: threads per block (0 = default 128; a
+ * multiple of 32 up to 256) and a kernel variant (0 = registers uncapped;
+ * 1.. = variants that cap registers for more resident warps, which launch
+ * 128-thread blocks).  gbds_op_num_variants gives the count.  Used by the
+ * autotuner. */
+int gbds_op_set_tuning(gbds_op op, int threads, int variant);
+int gbds_op_num_variants(gbds_op op);
 
 /* Number of kernels this library has launched in this process (all kinds). */
 long long gbds_kernel_launch_count(void);

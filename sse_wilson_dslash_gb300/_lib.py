@@ -54,7 +54,8 @@ def core() -> ctypes.CDLL:
     L.gbds_op_gauge_bytes.argtypes = [vp]
     L.gbds_op_gauge_bytes.restype = sz
     L.gbds_op_geometry.argtypes = [vp, c_int_p, c_int_p, c_int_p]
-    L.gbds_op_set_block.argtypes = [vp, i]
+    L.gbds_op_set_tuning.argtypes = [vp, i, i]
+    L.gbds_op_num_variants.argtypes = [vp]
     L.gbds_op_pack_gauge.argtypes = [vp, vp, vp, vp]
     L.gbds_op_pack_spinor.argtypes = [vp, vp, i, vp, vp]
     L.gbds_op_unpack_spinor.argtypes = [vp, vp, i, vp, vp]

@@ -100,6 +100,7 @@ extern "C" int gbds_op_create(gbds_op *op, const int dims[4], int nd, int prec, 
     o->prec = prec;
     o->recon = recon;
     o->block = 0;
+    o->variant = 0;
     o->d_site_table = nullptr;
     *op = o;
     return GBDS_SUCCESS;
@@ -154,13 +155,18 @@ extern "C" int gbds_op_geometry(gbds_op op, int *volume, int *volume_cb, int *st
     return GBDS_SUCCESS;
 }
 
-extern "C" int gbds_op_set_block(gbds_op op, int threads) {
+extern "C" int gbds_op_set_tuning(gbds_op op, int threads, int variant) {
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
     if (threads != 0 && (threads < 32 || threads > 256 || threads % 32 != 0))
         return set_error(GBDS_ERROR_INVALID_VALUE, "block must be 0 or a multiple of 32 in [32, 256]");
+    if (variant < 0 || variant >= dslash_variants(op->prec))
+        return set_error(GBDS_ERROR_INVALID_VALUE, "variant out of range");
     op->block = threads;
+    op->variant = variant;
     return GBDS_SUCCESS;
 }
+
+extern "C" int gbds_op_num_variants(gbds_op op) { return op ? dslash_variants(op->prec) : 0; }
 
 extern "C" int gbds_op_pack_gauge(gbds_op op, const void *u_packed, void *gauge, void *stream) {
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
@@ -202,8 +208,8 @@ extern "C" int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, vo
     if (!aligned16(gauge) || !aligned16(psi) || !aligned16(res))
         return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = op->prec == 32 ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, s)
-                                   : launch_dslash_f64(op->g, op->recon, gauge, psi, res, isign, cb, op->block, s);
+    cudaError_t e = op->prec == 32 ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)
+                                   : launch_dslash_f64(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
 }
 
@@ -374,8 +380,8 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
         if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_psi_packed, src, (size_t)g.Vh * spinor, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_pack_spinor(g, prec, c.d_psi_packed, nullptr, cb * g.Vh, cb, c.d_psi, s);
         if (e == cudaSuccess)
-            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, s)
-                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, s);
+            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s)
+                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
         if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, nullptr, target * g.Vh, target, c.d_res_packed, s);
         char *dst = static_cast<char *>(res) + (size_t)target * g.Vh * spinor;
         if (e == cudaSuccess) e = cudaMemcpyAsync(dst, c.d_res_packed, (size_t)g.Vh * spinor, cudaMemcpyDeviceToHost, s);
@@ -386,8 +392,8 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
         if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_res_packed, res, (size_t)g.V * spinor, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_pack_spinor(g, prec, c.d_psi_packed, table, 0, cb, c.d_psi, s);
         if (e == cudaSuccess)
-            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, s)
-                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, s);
+            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s)
+                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
         if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, table, 0, target, c.d_res_packed, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(res, c.d_res_packed, (size_t)g.V * spinor, cudaMemcpyDeviceToHost, s);
     }

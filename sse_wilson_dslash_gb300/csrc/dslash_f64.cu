@@ -3,7 +3,7 @@
 
 namespace gbds {
 cudaError_t launch_dslash_f64(const Geom &g, int recon, const void *gauge, const void *psi, void *res,
-                              int isign, int cb, int block, cudaStream_t stream) {
-    return launch_dslash_t<double>(g, recon, gauge, psi, res, isign, cb, block, stream);
+                              int isign, int cb, int block, int variant, cudaStream_t stream) {
+    return launch_dslash_t<double>(g, recon, gauge, psi, res, isign, cb, block, variant, stream);
 }
 }  // namespace gbds

@@ -293,8 +293,13 @@ __device__ __forceinline__ void hop_pair(const DslashArgs<T> &a, int h, const Nb
     reconstruct<MU, -ISIGN>(acc, w);
 }
 
-template <typename T, int ND, int RECON, int ISIGN>
-__global__ void __launch_bounds__(256) dslash_kernel(const DslashArgs<T> a) {
+// MINB > 0 caps registers so that MINB blocks of 128 threads fit on an SM
+// (launch with 128 threads); MINB == 0 leaves registers uncapped (<= 256 threads).
+template <int MINB> struct Bounds { static constexpr int threads = 128, blocks = MINB; };
+template <> struct Bounds<0> { static constexpr int threads = 256, blocks = 1; };
+
+template <typename T, int ND, int RECON, int ISIGN, int MINB>
+__global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks) dslash_kernel(const DslashArgs<T> a) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= a.g.Vh) return;
     Nbr n;
@@ -311,9 +316,50 @@ __global__ void __launch_bounds__(256) dslash_kernel(const DslashArgs<T> a) {
     Field<T>::store_spinor(a.res, a.g.stride, h, acc);
 }
 
+// Register-cap variants: index -> MINB (see Bounds).  FP32 and FP64 differ.
+template <typename T> struct Variants;
+template <> struct Variants<float> { static constexpr int n = 5; static constexpr int minb[5] = {0, 6, 7, 8, 10}; };
+template <> struct Variants<double> { static constexpr int n = 3; static constexpr int minb[3] = {0, 3, 4}; };
+
+template <typename T, int MINB>
+void launch_variant(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, cudaStream_t stream) {
+#define GBDS_LAUNCH(ND, R, S) dslash_kernel<T, ND, R, S, MINB><<<grid, block, 0, stream>>>(a)
+    if (nd == 4) {
+        if (recon == 18) { if (isign > 0) GBDS_LAUNCH(4, 18, 1); else GBDS_LAUNCH(4, 18, -1); }
+        else             { if (isign > 0) GBDS_LAUNCH(4, 12, 1); else GBDS_LAUNCH(4, 12, -1); }
+    } else {
+        if (recon == 18) { if (isign > 0) GBDS_LAUNCH(3, 18, 1); else GBDS_LAUNCH(3, 18, -1); }
+        else             { if (isign > 0) GBDS_LAUNCH(3, 12, 1); else GBDS_LAUNCH(3, 12, -1); }
+    }
+#undef GBDS_LAUNCH
+}
+
+template <typename T>
+void launch_minb(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, int minb, cudaStream_t s);
+
+template <>
+inline void launch_minb<float>(const DslashArgs<float> &a, dim3 grid, int block, int nd, int recon, int isign, int minb,
+                               cudaStream_t s) {
+    switch (minb) {
+    case 6: launch_variant<float, 6>(a, grid, block, nd, recon, isign, s); break;
+    case 7: launch_variant<float, 7>(a, grid, block, nd, recon, isign, s); break;
+    case 8: launch_variant<float, 8>(a, grid, block, nd, recon, isign, s); break;
+    default: launch_variant<float, 10>(a, grid, block, nd, recon, isign, s); break;
+    }
+}
+
+template <>
+inline void launch_minb<double>(const DslashArgs<double> &a, dim3 grid, int block, int nd, int recon, int isign,
+                                int minb, cudaStream_t s) {
+    switch (minb) {
+    case 3: launch_variant<double, 3>(a, grid, block, nd, recon, isign, s); break;
+    default: launch_variant<double, 4>(a, grid, block, nd, recon, isign, s); break;
+    }
+}
+
 template <typename T>
 cudaError_t launch_dslash_t(const Geom &g, int recon, const void *gauge, const void *psi, void *res,
-                            int isign, int cb, int block, cudaStream_t stream) {
+                            int isign, int cb, int block, int variant, cudaStream_t stream) {
     DslashArgs<T> a;
     a.g = g;
     a.psi = static_cast<const typename VecOf<T>::S *>(psi);
@@ -322,17 +368,14 @@ cudaError_t launch_dslash_t(const Geom &g, int recon, const void *gauge, const v
     const int vec_bytes = sizeof(T) == 4 ? (recon == 18 ? 8 : 16) : 16;
     a.link_block_bytes = (size_t)Field<T>::link_vecs(recon) * g.stride * vec_bytes;
     a.pt = 1 - cb;
+    if (variant < 0 || variant >= Variants<T>::n) variant = 0;
     if (block <= 0) block = 128;
+    if (Variants<T>::minb[variant] > 0) block = 128;  // the register cap assumes 128-thread blocks
     const dim3 grid((g.Vh + block - 1) / block);
-#define GBDS_LAUNCH(ND, R, S) dslash_kernel<T, ND, R, S><<<grid, block, 0, stream>>>(a)
-    if (g.nd == 4) {
-        if (recon == 18) { if (isign > 0) GBDS_LAUNCH(4, 18, 1); else GBDS_LAUNCH(4, 18, -1); }
-        else             { if (isign > 0) GBDS_LAUNCH(4, 12, 1); else GBDS_LAUNCH(4, 12, -1); }
-    } else {
-        if (recon == 18) { if (isign > 0) GBDS_LAUNCH(3, 18, 1); else GBDS_LAUNCH(3, 18, -1); }
-        else             { if (isign > 0) GBDS_LAUNCH(3, 12, 1); else GBDS_LAUNCH(3, 12, -1); }
+    switch (Variants<T>::minb[variant]) {
+    case 0: launch_variant<T, 0>(a, grid, block, g.nd, recon, isign, stream); break;
+    default: launch_minb<T>(a, grid, block, g.nd, recon, isign, Variants<T>::minb[variant], stream); break;
     }
-#undef GBDS_LAUNCH
     count_launch();
     return cudaGetLastError();
 }

@@ -28,10 +28,13 @@ void count_launch(int n = 1);
 
 // Launchers (defined in dslash_f32.cu / dslash_f64.cu / layout.cu).
 // All pointers are device pointers; `stream` is a cudaStream_t.
+// block: threads per block (0 = default); variant: register-cap variant
+// (0 = uncapped; see Variants<T> in dslash_kernel.cuh).
 cudaError_t launch_dslash_f32(const Geom &g, int recon, const void *gauge, const void *psi,
-                              void *res, int isign, int cb, int block, cudaStream_t stream);
+                              void *res, int isign, int cb, int block, int variant, cudaStream_t stream);
 cudaError_t launch_dslash_f64(const Geom &g, int recon, const void *gauge, const void *psi,
-                              void *res, int isign, int cb, int block, cudaStream_t stream);
+                              void *res, int isign, int cb, int block, int variant, cudaStream_t stream);
+int dslash_variants(int prec);
 
 // site0: first caller site held by the packed buffer (0 for a full lattice).
 cudaError_t launch_pack_spinor(const Geom &g, int prec, const void *psi_packed, const int *site_table,
@@ -55,5 +58,6 @@ struct gbds_op_s {
     int prec;
     int recon;
     int block;
+    int variant;
     int *d_site_table;  // device copy of the layout table, or nullptr (canonical)
 };

@@ -84,7 +84,7 @@ extern "C" int gbds_dslash_packed_noalloc_f32(const int dims[4], int nd, const f
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = gbds::launch_pack_gauge(g, 32, 18, u_packed, nullptr, gauge, st);
     if (e == cudaSuccess) e = gbds::launch_pack_spinor(g, 32, psi_packed, nullptr, 0, cb, src, st);
-    if (e == cudaSuccess) e = gbds::launch_dslash_f32(g, 18, gauge, src, dst, isign, cb, 0, st);
+    if (e == cudaSuccess) e = gbds::launch_dslash_f32(g, 18, gauge, src, dst, isign, cb, 0, 0, st);
     if (e == cudaSuccess) e = gbds::launch_unpack_spinor(g, 32, dst, nullptr, 0, 1 - cb, res_packed, st);
     return e == cudaSuccess ? GBDS_SUCCESS : gbds::cuda_error(e, "gbds_dslash_packed_noalloc_f32");
 }

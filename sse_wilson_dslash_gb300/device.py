@@ -77,8 +77,12 @@ class DslashOperator:
     def canonical(self) -> bool:
         return bool(_lib.core().gbds_op_is_canonical(self._h))
 
-    def set_block(self, threads: int) -> None:
-        _lib.check(_lib.core().gbds_op_set_block(self._h, int(threads)))
+    def set_tuning(self, threads: int, variant: int = 0) -> None:
+        _lib.check(_lib.core().gbds_op_set_tuning(self._h, int(threads), int(variant)))
+
+    @property
+    def num_variants(self) -> int:
+        return int(_lib.core().gbds_op_num_variants(self._h))
 
     # -- fields ----------------------------------------------------------------
     def new_spinor(self):

@@ -69,7 +69,9 @@ def test_op_create_validation(libs):
             real = prec // 8
             assert L.gbds_op_spinor_bytes(h) == 24 * real * st.value
             assert L.gbds_op_gauge_bytes(h) == 2 * nd * recon * real * st.value
-            assert L.gbds_op_set_block(h, 96) == 0 and L.gbds_op_set_block(h, 100) != 0
+            assert L.gbds_op_set_tuning(h, 96, 0) == 0 and L.gbds_op_set_tuning(h, 100, 0) != 0
+            nv = L.gbds_op_num_variants(h)
+            assert nv >= 2 and L.gbds_op_set_tuning(h, 0, nv - 1) == 0 and L.gbds_op_set_tuning(h, 0, nv) != 0
             L.gbds_op_destroy(h)
         else:
             assert L.gbds_get_last_error()
