@@ -176,11 +176,12 @@ def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None):
     gauge = op.pack_gauge(u)
     srcs = [op.pack_spinor(psi, 0), op.pack_spinor(psi, 1)]
     outs = [op.new_spinor(), op.new_spinor()]
+    tuning = op.autotune(gauge, srcs[0], outs[1])
     ms = time_device(op, gauge, srcs, outs, steps, warmup, torch)
     sites = op.volume_cb
     res = {"ms": ms, "gflops": op.flops_per_site * sites / (ms * 1e6),
            "gbs": op.bytes_per_site * sites / (ms * 1e6), "bytes_per_site": op.bytes_per_site,
-           "flops_per_site": op.flops_per_site, "sites": sites}
+           "flops_per_site": op.flops_per_site, "sites": sites, "tuning": list(tuning)}
     del gauge, srcs, outs
     op.close()
     return res
@@ -327,6 +328,7 @@ def run_gb300(args):
     gauge = op.pack_gauge(u)
     srcs = [op.pack_spinor(psi, 0), op.pack_spinor(psi, 1)]
     outs = [op.new_spinor(), op.new_spinor()]
+    tuning = op.autotune(gauge, srcs[0], outs[1])
     stream = torch.cuda.current_stream()
     combos = [(1, 0), (-1, 1), (-1, 0), (1, 1)]
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
@@ -400,12 +402,25 @@ def run_gb300(args):
         torch.cuda.synchronize()
         barrier()
         dt = time.perf_counter() - t0
+        from sse_wilson_dslash_gb300 import legacy
+        path = "direct (kernels read/write the pinned host arrays over NVLink-C2C)" if legacy.last_path() == 1 \
+            else "staged (cudaMemcpyAsync)"
         e2e = {"value": FLOPS_4D * sites * e2e_steps * world / dt / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": op.volume * 72 * 4 + sites * 96, "d2h_bytes_per_step": sites * 96,
                "steps": e2e_steps, "ms_per_step": dt / e2e_steps * 1e3,
-               "path": "sse_su3dslash_wilson (libgbdslash32.so), pinned host arrays, gauge copied every call"}
+               "path": "sse_su3dslash_wilson (libgbdslash32.so), pinned host arrays, gauge read every call, "
+                       + path}
+        # the same calls staged through cudaMemcpyAsync, for comparison
+        legacy.set_host_access(1)
+        d.sse_su3dslash_wilson(u_h, psi_h, res_h, 1, 0)
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            isign, cb = combos[k % 4]
+            d.sse_su3dslash_wilson(u_h, psi_h, res_h, isign, cb)
+        dt_s = time.perf_counter() - t0
+        legacy.set_host_access(0)
+        e2e["staged"] = {"value": FLOPS_4D * sites * e2e_steps * world / dt_s / 1e9, "ms_per_step": dt_s / e2e_steps * 1e3}
         # gauge-resident variant: the caller promises u is unchanged between calls
-        from sse_wilson_dslash_gb300 import legacy
         legacy.set_gauge_cache(True)
         d.sse_su3dslash_wilson(u_h, psi_h, res_h, 1, 0)
         torch.cuda.synchronize()
@@ -455,7 +470,8 @@ def run_gb300(args):
                 "config": {"workload": WORKLOAD, "lattice": list(DIMS), "nd": 4, "prec": 32, "recon": 18,
                            "sites_per_step": sites, "flops_per_site": FLOPS_4D, "bytes_per_site": bytes_per_site,
                            "l2": "no flush: inputs (gauge 576 MiB, spinors 2 x 96 MiB) exceed the 129 MB L2",
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "tuning": {"block": tuning[0], "variant": tuning[1]}},
                 "hbm_gbs": achieved,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_source": peak_kind,

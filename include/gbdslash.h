@@ -120,7 +120,14 @@ int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
  * 128-thread blocks).  gbds_op_num_variants gives the count.  Used by the
  * autotuner. */
 int gbds_op_set_tuning(gbds_op op, int threads, int variant);
+int gbds_op_get_tuning(gbds_op op, int *threads, int *variant);
 int gbds_op_num_variants(gbds_op op);
+
+/* Time every (block, variant) candidate of gbds_op_dslash on the caller's
+ * fields (res is overwritten), keep the fastest for this operator and cache
+ * it process-wide for its (dims, nd, prec, recon); a later call for the same
+ * shape takes the cached choice without timing.  Synchronises `stream`. */
+int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream);
 
 /* Number of kernels this library has launched in this process (all kinds). */
 long long gbds_kernel_launch_count(void);
@@ -231,6 +238,17 @@ int gbds_legacy_invalidate_gauge(void);
  * 12 = two rows, third rebuilt; only valid for SU(3) links).  Default 18.
  * Takes effect at the next init. */
 int gbds_legacy_set_recon(int recon);
+
+/* How the legacy path reaches the caller's host arrays (canonical layouts):
+ * 0 (default) - where the GPU can address them (pinned or registered memory,
+ *               device or managed memory, or pageable memory on a host whose
+ *               pages the GPU translates, as on NVLink-C2C Grace systems) the
+ *               layout kernels read u/psi and write res in place;
+ *               otherwise as 1;
+ * 1           - stage every array through cudaMemcpyAsync. */
+int gbds_legacy_set_host_access(int mode);
+/* Path taken by the last legacy apply: 1 direct, 0 staged, -1 none yet. */
+int gbds_legacy_last_path(void);
 
 /* Refcount of a legacy context: prec 32/64, nd 4/3 (0 = not initialised). */
 int gbds_legacy_refcount(int prec, int nd);

@@ -56,11 +56,14 @@ def core() -> ctypes.CDLL:
     L.gbds_op_geometry.argtypes = [vp, c_int_p, c_int_p, c_int_p]
     L.gbds_op_set_tuning.argtypes = [vp, i, i]
     L.gbds_op_num_variants.argtypes = [vp]
+    L.gbds_op_get_tuning.argtypes = [vp, c_int_p, c_int_p]
+    L.gbds_op_autotune.argtypes = [vp, vp, vp, vp, vp]
     L.gbds_op_pack_gauge.argtypes = [vp, vp, vp, vp]
     L.gbds_op_pack_spinor.argtypes = [vp, vp, i, vp, vp]
     L.gbds_op_unpack_spinor.argtypes = [vp, vp, i, vp, vp]
     L.gbds_op_dslash.argtypes = [vp, vp, vp, vp, i, i, vp]
-    for n in ("gbds_legacy_set_exit_on_error", "gbds_legacy_set_gauge_cache", "gbds_legacy_set_recon"):
+    for n in ("gbds_legacy_set_exit_on_error", "gbds_legacy_set_gauge_cache", "gbds_legacy_set_recon",
+              "gbds_legacy_set_host_access"):
         getattr(L, n).argtypes = [i]
     L.gbds_legacy_refcount.argtypes = [i, i]
     L.gbds_layout_select.argtypes = [i, c_int_p]

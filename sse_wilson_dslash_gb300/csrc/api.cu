@@ -3,8 +3,11 @@
 // (init / free / apply / pack) behind precision-suffixed names.
 #include <cuda_runtime.h>
 
+#include <array>
 #include <atomic>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -99,8 +102,12 @@ extern "C" int gbds_op_create(gbds_op *op, const int dims[4], int nd, int prec, 
     o->g = g;
     o->prec = prec;
     o->recon = recon;
-    o->block = 0;
-    o->variant = 0;
+    // Defaults from a sweep on GB300 at 32^3x64 and 24^3x48 (gbds_op_autotune
+    // refines them per lattice): FP32 recon 18 runs best with registers capped
+    // for 6 blocks of 128 threads per SM, FP32 recon 12 with 64-thread blocks,
+    // FP64 (FP64-issue bound) is insensitive.
+    o->block = (prec == 32 && recon == 12) ? 64 : 128;
+    o->variant = (prec == 32 && recon == 18) ? 1 : 0;
     o->d_site_table = nullptr;
     *op = o;
     return GBDS_SUCCESS;
@@ -168,11 +175,69 @@ extern "C" int gbds_op_set_tuning(gbds_op op, int threads, int variant) {
 
 extern "C" int gbds_op_num_variants(gbds_op op) { return op ? dslash_variants(op->prec) : 0; }
 
+namespace {
+std::mutex g_tune_mutex;
+std::map<std::array<int, 7>, std::array<int, 2>> g_tune_cache;  // (dims, nd, prec, recon) -> (block, variant)
+}
+
+extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream) {
+    if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
+    const std::array<int, 7> key = {op->g.L[0], op->g.L[1], op->g.L[2], op->g.L[3], op->g.nd, op->prec, op->recon};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            op->block = it->second[0];
+            op->variant = it->second[1];
+            return GBDS_SUCCESS;
+        }
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::vector<std::array<int, 2>> cand = {{64, 0}, {128, 0}, {256, 0}};
+    for (int v = 1; v < dslash_variants(op->prec); v++) cand.push_back({128, v});
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) return cuda_error(e, "autotune events");
+    float best = 1e30f;
+    std::array<int, 2> pick = {op->block, op->variant};
+    const int reps = op->prec == 32 ? 10 : 3;
+    for (const auto &c : cand) {
+        op->block = c[0];
+        op->variant = c[1];
+        int rc = gbds_op_dslash(op, gauge, psi, res, 1, 0, stream);  // warm-up
+        if (rc != GBDS_SUCCESS) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < reps; r++) gbds_op_dslash(op, gauge, psi, res, (r & 1) ? -1 : 1, 0, stream);
+        cudaEventRecord(e1, s);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; pick = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_error(e, "autotune");
+    op->block = pick[0];
+    op->variant = pick[1];
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = pick;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_op_get_tuning(gbds_op op, int *threads, int *variant) {
+    if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
+    if (threads) *threads = op->block;
+    if (variant) *variant = op->variant;
+    return GBDS_SUCCESS;
+}
+
 extern "C" int gbds_op_pack_gauge(gbds_op op, const void *u_packed, void *gauge, void *stream) {
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
     if (!u_packed || !gauge) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL field pointer");
     if (!aligned16(gauge)) return set_error(GBDS_ERROR_INVALID_VALUE, "gauge must be 16-byte aligned");
-    if (op->prec == 64 && (reinterpret_cast<uintptr_t>(u_packed) & 7u))
+    if (reinterpret_cast<uintptr_t>(u_packed) & 7u)
         return set_error(GBDS_ERROR_INVALID_VALUE, "u_packed must be 8-byte aligned");
     cudaError_t e = launch_pack_gauge(op->g, op->prec, op->recon, u_packed, op->d_site_table, gauge,
                                       static_cast<cudaStream_t>(stream));
@@ -237,6 +302,32 @@ LegacyCtx g_legacy[2][2];  // [prec 32 -> 0, 64 -> 1][nd 4 -> 0, 3 -> 1]
 int g_exit_on_error = 1;
 int g_gauge_cache = 0;
 int g_legacy_recon = 18;
+int g_host_access = 0;  // 0: read/write host arrays directly where the GPU can; 1: always stage
+int g_last_path = -1;   // 0 staged, 1 direct
+
+// Address under which kernels can use a caller array, or nullptr when the
+// GPU cannot reach it directly.  Pinned / registered host memory has a device
+// view; on a coherent host (NVLink-C2C with address translation services) the
+// GPU reads pageable memory through the host page tables; device and managed
+// pointers are usable as they are.
+const void *device_view(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    switch (a.type) {
+    case cudaMemoryTypeDevice:
+    case cudaMemoryTypeManaged: return p;
+    case cudaMemoryTypeHost: return a.devicePointer;
+    default: break;
+    }
+    int dev = 0, pageable = 0, ats = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    return (pageable && ats) ? p : nullptr;
+}
 
 LegacyCtx &ctx_for(int prec, int nd) { return g_legacy[prec == 32 ? 0 : 1][nd == 4 ? 0 : 1]; }
 
@@ -369,6 +460,37 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
     const int *table = c.op->d_site_table;
     cudaError_t e = cudaSuccess;
     const bool reuse_gauge = g_gauge_cache && c.cached_u == u;
+    const void *du = nullptr, *dpsi = nullptr;
+    void *dres = nullptr;
+    if (c.canonical && g_host_access == 0) {
+        du = reuse_gauge ? u : device_view(u);
+        dpsi = device_view(psi);
+        dres = const_cast<void *>(device_view(res));
+    }
+    const bool aligned = ((reinterpret_cast<uintptr_t>(du) | reinterpret_cast<uintptr_t>(dpsi) |
+                           reinterpret_cast<uintptr_t>(dres)) & 15u) == 0;
+    if (du && dpsi && dres && aligned) {
+        // Direct: the layout kernels read u and psi and write res where they
+        // lie, with no intermediate copy.
+        if (!reuse_gauge) {
+            e = launch_pack_gauge(g, prec, c.op->recon, du, nullptr, c.d_gauge, s);
+            c.cached_u = e == cudaSuccess ? u : nullptr;
+        }
+        if (e == cudaSuccess) e = launch_pack_spinor(g, prec, dpsi, nullptr, 0, cb, c.d_psi, s);
+        if (e == cudaSuccess)
+            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s)
+                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
+        if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, nullptr, 0, target, dres, s);
+        cudaError_t e2 = cudaStreamSynchronize(s);
+        if (e == cudaSuccess) e = e2;
+        g_last_path = 1;
+        if (e != cudaSuccess) {
+            c.cached_u = nullptr;
+            fprintf(stderr, "%s: CUDA error: %s\n", fn, cudaGetErrorString(e));
+        }
+        return;
+    }
+    g_last_path = 0;
     if (!reuse_gauge) {
         e = cudaMemcpyAsync(c.d_u_packed, u, (size_t)g.V * 4 * 18 * real, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = launch_pack_gauge(g, prec, c.op->recon, c.d_u_packed, table, c.d_gauge, s);
@@ -478,6 +600,14 @@ extern "C" int gbds_legacy_set_recon(int recon) {
     g_legacy_recon = recon;
     return GBDS_SUCCESS;
 }
+
+extern "C" int gbds_legacy_set_host_access(int mode) {
+    if (mode != 0 && mode != 1) return set_error(GBDS_ERROR_INVALID_VALUE, "mode must be 0 (direct where possible) or 1 (staged)");
+    g_host_access = mode;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_legacy_last_path(void) { return g_last_path; }
 
 extern "C" int gbds_legacy_refcount(int prec, int nd) {
     if ((prec != 32 && prec != 64) || (nd != 3 && nd != 4)) return -1;

@@ -80,6 +80,17 @@ class DslashOperator:
     def set_tuning(self, threads: int, variant: int = 0) -> None:
         _lib.check(_lib.core().gbds_op_set_tuning(self._h, int(threads), int(variant)))
 
+    def tuning(self):
+        b, v = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.core().gbds_op_get_tuning(self._h, ctypes.byref(b), ctypes.byref(v)))
+        return b.value, v.value
+
+    def autotune(self, gauge, psi, scratch, stream=None):
+        """Pick the fastest launch configuration on these fields (scratch is overwritten)."""
+        _lib.check(_lib.core().gbds_op_autotune(self._h, ctypes.c_void_p(_dptr(gauge)), ctypes.c_void_p(_dptr(psi)),
+                                                ctypes.c_void_p(_dptr(scratch)), _stream(stream)))
+        return self.tuning()
+
     @property
     def num_variants(self) -> int:
         return int(_lib.core().gbds_op_num_variants(self._h))

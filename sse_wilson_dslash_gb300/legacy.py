@@ -107,6 +107,16 @@ def set_recon(recon: int) -> None:
     _lib.check(_lib.core().gbds_legacy_set_recon(int(recon)))
 
 
+def set_host_access(mode: int) -> None:
+    """0: kernels read/write the caller's host arrays directly where possible; 1: stage copies."""
+    _lib.check(_lib.core().gbds_legacy_set_host_access(int(mode)))
+
+
+def last_path() -> int:
+    """1 if the last apply used direct host access, 0 if it staged copies."""
+    return int(_lib.core().gbds_legacy_last_path())
+
+
 def refcount(prec: int, nd: int) -> int:
     return int(_lib.core().gbds_legacy_refcount(prec, nd))
 

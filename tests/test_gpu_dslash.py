@@ -36,16 +36,19 @@ def _apply(d, nd, u, psi, res, isign, cb):
     (d.sse_su3dslash_wilson if nd == 4 else d.sse_su3dslash_wilson_3d)(u, psi, res, isign, cb)
 
 
-@pytest.mark.parametrize("recon", [18, 12])
+@pytest.mark.parametrize("recon,access", [(18, 0), (18, 1), (12, 0)])
 @pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("name", CASES)
-def test_dropin_matches_reference_golden(dropin, name, prec, recon):
+def test_dropin_matches_reference_golden(dropin, name, prec, recon, access):
+    """access 0: kernels read/write the host arrays directly where the GPU can
+    reach them; 1: staged through cudaMemcpyAsync."""
     from sse_wilson_dslash_gb300 import legacy
     c = MAN["cases"][name]
     dims, nd = tuple(c["dims"]), c["nd"]
     kind, lol = layout(c, dims)
     d = dropin[prec]
     legacy.set_recon(recon)
+    legacy.set_host_access(access)
     try:
         _init(d, nd, dims, kind, lol)
         u, psi = O.make_inputs(dims, MAN["seeds"]["gauge"], MAN["seeds"]["spinor"], c["gauge"])
@@ -61,9 +64,12 @@ def test_dropin_matches_reference_golden(dropin, name, prec, recon):
                 check_against_golden(MAN, ARR, name, prec, isign, cb, res)
                 ref = O.dslash_plain(nd, dims, lol, u, psi, isign, cb)
                 assert O.site_rel_err(res, ref, O.target_sites(nd, dims, lol, cb)) <= SITE_TOL[prec]
+        if access == 1 or kind == O.LAYOUT_PERM or kind == O.LAYOUT_LEX:
+            assert legacy.last_path() == 0
     finally:
         _free(d, nd)
         legacy.set_recon(18)
+        legacy.set_host_access(0)
 
 
 def test_refcount_keeps_first_lattice(dropin):
@@ -129,6 +135,58 @@ def test_edge_lattices(dropin, nd, dims, prec):
                 assert O.site_rel_err(res, ref, O.target_sites(nd, dims, lol, cb)) <= SITE_TOL[prec]
     finally:
         _free(d, nd)
+
+
+def test_pinned_host_arrays_take_the_direct_path(dropin):
+    """Pinned host arrays are read and written in place by the layout kernels."""
+    import torch
+    from sse_wilson_dslash_gb300 import legacy
+    d = dropin[32]
+    dims = (8, 4, 4, 8)
+    _init(d, 4, dims, O.LAYOUT_CB2, None)
+    try:
+        u, psi = O.make_inputs(dims, 31, 32)
+        V = O.volume(dims)
+        ut = torch.from_numpy(u.astype(np.float32).ravel()).pin_memory()
+        pt = torch.from_numpy(psi.astype(np.float32).ravel()).pin_memory()
+        rt = torch.full((V * 24,), 2.5, dtype=torch.float32).pin_memory()
+        legacy.set_gauge_cache(True)
+        lol = O.layout_table(O.LAYOUT_CB2, dims)
+        for isign, cb in ((1, 0), (-1, 1), (1, 1)):
+            d.sse_su3dslash_wilson(ut, pt, rt, isign, cb)
+            assert legacy.last_path() == 1
+            res = rt.numpy().reshape(V, 4, 3, 2).copy()
+            ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), psi.astype(np.float32), isign, cb)
+            assert O.site_rel_err(res, ref, O.target_sites(4, dims, lol, cb)) <= 1e-6
+        # gauge cache: a changed field behind the same pointer is only seen after invalidation
+        ut.mul_(-1.0)
+        legacy.invalidate_gauge()
+        d.sse_su3dslash_wilson(ut, pt, rt, 1, 0)
+        ref = O.dslash_plain(4, dims, lol, -u.astype(np.float32), psi.astype(np.float32), 1, 0)
+        assert O.site_rel_err(rt.numpy().reshape(V, 4, 3, 2), ref, O.target_sites(4, dims, lol, 0)) <= 1e-6
+    finally:
+        legacy.set_gauge_cache(False)
+        _free(d, 4)
+
+
+def test_autotune_picks_a_valid_configuration_and_keeps_results():
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims = (16, 8, 8, 8)
+    op = DslashOperator(dims, nd=4, prec=32, recon=18)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    u = torch.randn(op.volume * 72, device="cuda", generator=g)
+    psi = torch.randn(op.volume * 24, device="cuda", generator=g)
+    gauge = op.pack_gauge(u)
+    src = op.pack_spinor(psi, 0)
+    before = op.apply(gauge, src, 1, 0).clone()
+    block, variant = op.autotune(gauge, src, op.new_spinor())
+    assert block % 32 == 0 and 0 <= variant < op.num_variants
+    after = op.apply(gauge, src, 1, 0)
+    torch.cuda.synchronize()
+    assert torch.equal(before, after)
+    op2 = DslashOperator(dims, nd=4, prec=32, recon=18)
+    assert op2.autotune(gauge, src, op.new_spinor()) == (block, variant)  # cached per shape
 
 
 # ---------------------------------------------------------------------------
