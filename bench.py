@@ -138,6 +138,60 @@ def su3_links(n, gen, torch):
     return out
 
 
+def near_unit_links(n, gen, torch, eps=0.3):
+    """n matrices exp(i*eps*H), H traceless Hermitian with N(0,1) entries,
+    packed [n][j][i][2] (transposed), float64."""
+    out = torch.empty(n, 3, 3, 2, dtype=torch.float64, device="cuda")
+    chunk = 1 << 21
+    iu = torch.triu_indices(3, 3, 1, device="cuda")
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        d = torch.randn(m, 3, dtype=torch.float64, device="cuda", generator=gen)
+        od = torch.randn(m, 3, 2, dtype=torch.float64, device="cuda", generator=gen)
+        H = torch.zeros(m, 3, 3, dtype=torch.complex128, device="cuda")
+        H.diagonal(dim1=1, dim2=2).copy_((d - d.mean(1, keepdim=True)).to(torch.complex128))
+        off = torch.view_as_complex(od)
+        H[:, iu[0], iu[1]] = off
+        H[:, iu[1], iu[0]] = off.conj()
+        U = torch.linalg.matrix_exp(1j * eps * H)
+        out[s:s + m] = torch.view_as_real(U.transpose(1, 2).contiguous())
+    return out
+
+
+def run_solver_bench(torch, log_fn):
+    """Time to |c - A x| <= 1e-10 |c| for the even-odd Wilson operator,
+    kappa = 0.124, 32^3x64, near-unit links: all-FP64 CG vs FP32 CG inside FP64
+    defect correction."""
+    from sse_wilson_dslash_gb300.device import WilsonSolver
+    dims = (32, 32, 32, 64)
+    V = dims[0] * dims[1] * dims[2] * dims[3]
+    gen = torch.Generator(device="cuda").manual_seed(99)
+    u = near_unit_links(V * 4, gen, torch).reshape(-1)
+    b = torch.randn(V * 24, dtype=torch.float64, device="cuda", generator=gen)
+    out = {"lattice": list(dims), "kappa": 0.124, "links": "exp(i 0.3 H), H traceless Hermitian N(0,1)",
+           "source": "N(0,1)", "tol": 1e-10, "residual": "|M^+ b - M^+ M x| / |M^+ b| (CG on M^+ M)"}
+    sols = {}
+    for name, prec, recon in (("fp64_cg", 64, 18), ("mixed_fp32_fp64", 32, 12)):
+        s = WilsonSolver(dims, 0.124, tol=1e-10, max_iter=20000, inner_prec=prec, inner_recon=recon, inner_tol=1e-5)
+        s.set_gauge(u)
+        x = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = s.solve(b, x)
+        torch.cuda.synchronize()
+        st["wall_seconds"] = time.perf_counter() - t0
+        st["inner_recon"] = recon
+        out[name] = st
+        sols[name] = x
+        log_fn(name, st)
+        s.close()
+        del s
+        torch.cuda.empty_cache()
+    out["speedup"] = out["fp64_cg"]["wall_seconds"] / out["mixed_fp32_fp64"]["wall_seconds"]
+    out["solution_rel_diff"] = float((sols["fp64_cg"] - sols["mixed_fp32_fp64"]).norm() / sols["fp64_cg"].norm())
+    return out
+
+
 def make_fields(dims, dtype, torch, seed=1234):
     V = dims[0] * dims[1] * dims[2] * dims[3]
     gen = torch.Generator(device="cuda").manual_seed(seed)
@@ -462,6 +516,11 @@ def run_gb300(args):
         for v in variants.values():
             v["roofline_frac"] = v["gbs"] / peak
 
+    solver = None
+    if not args.no_solver:
+        torch.cuda.empty_cache()
+        solver = run_solver_bench(torch, log)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -479,7 +538,7 @@ def run_gb300(args):
                              "kernel": "gbds::dslash_kernel<float,4,18,isign>"},
                 "gflops_ref_convention": 1390 * sites / (ms * 1e6),
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
-                "variants": variants}
+                "variants": variants, "solver": solver}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -497,6 +556,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-solver", action="store_true")
     ap.add_argument("--dims", default=None,
                     help="Lx,Ly,Lz,Lt of the 4D workload (default 32,32,32,64; smaller cases are for profiling)")
     args = ap.parse_args()

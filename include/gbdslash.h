@@ -167,6 +167,49 @@ int gbds_dslash_packed_noalloc_f32(const int dims[4], int nd, const float *u_pac
                                    float *res_packed, int isign, int cb, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Even-odd preconditioned Wilson solver                                     */
+/* ------------------------------------------------------------------------ */
+/* M = 1 - kappa^2 D_eo D_oe on checkerboard 0 (even sites), D the operator
+ * above (D_oe: cb = 0 source, D_eo: cb = 1 source); M^+ uses isign = -1.
+ * CG on A = M^+ M, right-hand side c = M^+ b.  No counterpart in the
+ * reference, which provides only D; its callers (Chroma) build M and the
+ * solvers around it. */
+
+typedef struct gbds_solver_s *gbds_solver;
+
+typedef struct gbds_solver_params {
+    double kappa;     /* hopping parameter */
+    double tol;       /* stop when |c - A x| <= tol |c| (FP64) */
+    int max_iter;     /* CG iterations, all cycles together */
+    int inner_prec;   /* 64: all-FP64 CG; 32: FP32 CG inside FP64 defect correction */
+    int inner_recon;  /* 18 or 12: gauge compression of the FP32 operator */
+    double inner_tol; /* residual reduction per defect-correction cycle (e.g. 1e-5) */
+} gbds_solver_params;
+
+typedef struct gbds_solver_stats {
+    int iterations;       /* CG iterations in total */
+    int cycles;           /* defect-correction cycles (1 for FP64 CG) */
+    int converged;        /* residual <= tol */
+    double residual;      /* |c - A x| / |c|, recomputed in FP64 at the end */
+    double true_residual; /* |b - M x| / |b|, FP64 */
+    double seconds;       /* wall time of the solve, including its syncs */
+} gbds_solver_stats;
+
+/* Allocates its fields on the current device. */
+int gbds_solver_create(gbds_solver *s, const int dims[4], const gbds_solver_params *p);
+int gbds_solver_destroy(gbds_solver s);
+/* u_packed: FP64 device array [V][4][3][3][2] (reference layout, QDP++ cb2
+ * order); kept in FP64 for the outer residual and in FP32 for the inner CG. */
+int gbds_solver_set_gauge(gbds_solver s, const double *u_packed, void *stream);
+/* y = M x (dagger = 0) or M^+ x (dagger = 1) on the even sites of FP64
+ * device arrays [V][4][3][2] in cb2 order; odd sites of y are not written. */
+int gbds_solver_apply(gbds_solver s, const double *x_packed, double *y_packed, int dagger, void *stream);
+/* Solve M x = b on the even sites (b, x as in gbds_solver_apply; x is
+ * written on the even sites only; it starts from zero). */
+int gbds_solver_solve(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats,
+                      void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Reference entry points with precision suffixes                            */
 /* ------------------------------------------------------------------------ */
 /* Same arguments and behaviour as init_sse_su3dslash & co.

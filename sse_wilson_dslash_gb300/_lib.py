@@ -20,6 +20,18 @@ GETLINEAR = ctypes.CFUNCTYPE(ctypes.c_int, c_int_p)
 NODENUM = ctypes.CFUNCTYPE(ctypes.c_int, c_int_p)
 
 
+class SolverParams(ctypes.Structure):
+    """gbds_solver_params (include/gbdslash.h)."""
+    _fields_ = [("kappa", ctypes.c_double), ("tol", ctypes.c_double), ("max_iter", ctypes.c_int),
+                ("inner_prec", ctypes.c_int), ("inner_recon", ctypes.c_int), ("inner_tol", ctypes.c_double)]
+
+
+class SolverStats(ctypes.Structure):
+    """gbds_solver_stats (include/gbdslash.h)."""
+    _fields_ = [("iterations", ctypes.c_int), ("cycles", ctypes.c_int), ("converged", ctypes.c_int),
+                ("residual", ctypes.c_double), ("true_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
 class GbdsError(RuntimeError):
     """A gbds_* call returned a non-zero status."""
 
@@ -67,6 +79,11 @@ def core() -> ctypes.CDLL:
         getattr(L, n).argtypes = [i]
     L.gbds_legacy_refcount.argtypes = [i, i]
     L.gbds_layout_select.argtypes = [i, c_int_p]
+    L.gbds_solver_create.argtypes = [ctypes.POINTER(vp), c_int_p, ctypes.POINTER(SolverParams)]
+    L.gbds_solver_destroy.argtypes = [vp]
+    L.gbds_solver_set_gauge.argtypes = [vp, vp, vp]
+    L.gbds_solver_apply.argtypes = [vp, vp, vp, i, vp]
+    L.gbds_solver_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
     _core = L
     return L
 

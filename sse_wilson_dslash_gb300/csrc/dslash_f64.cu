@@ -6,4 +6,8 @@ cudaError_t launch_dslash_f64(const Geom &g, int recon, const void *gauge, const
                               int isign, int cb, int block, int variant, cudaStream_t stream) {
     return launch_dslash_t<double>(g, recon, gauge, psi, res, isign, cb, block, variant, stream);
 }
+cudaError_t launch_dslash_xpay_f64(const Geom &g, int recon, const void *gauge, const void *psi, const void *x,
+                                   double coef, void *res, double *partials, int isign, int cb, cudaStream_t stream) {
+    return launch_dslash_xpay_t<double>(g, recon, gauge, psi, x, coef, res, partials, isign, cb, stream);
+}
 }  // namespace gbds

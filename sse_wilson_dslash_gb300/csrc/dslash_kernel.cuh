@@ -334,6 +334,100 @@ void launch_variant(const DslashArgs<T> &a, dim3 grid, int block, int nd, int re
 #undef GBDS_LAUNCH
 }
 
+// ---------------------------------------------------------------------------
+// Dslash with an xpay epilogue and a norm reduction, for the even-odd
+// operator M = 1 - kappa^2 D_eo D_oe:  out = x + coef * Dslash(psi), and
+// partials[block] = sum over the block's sites of |out|^2 (for the CG's
+// <p, M^+M p> = |M p|^2).  4D only.
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ void load_spinor_any(const typename VecOf<T>::S *p, int stride, int h, cx<T> (&s)[4][3]) {
+    Field<T>::load_spinor(p, stride, h, s);
+}
+
+// Sum a per-thread float/double over the block into partials[blockIdx.x] (double).
+template <typename T>
+__device__ __forceinline__ void block_sum_to(double *partials, T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __shared__ double warp_sums[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) warp_sums[w] = (double)v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int i = 0; i < nw; i++) t += warp_sums[i];
+        partials[blockIdx.x] = t;
+    }
+}
+
+template <typename T, int RECON, int ISIGN, int MINB>
+__global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks)
+    dslash_xpay_kernel(const DslashArgs<T> a, const typename VecOf<T>::S *__restrict__ x, T coef, double *partials) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    T nrm = 0;
+    if (h < a.g.Vh) {
+        Nbr n;
+        neighbours<4>(a.g, h, a.pt, n);
+        cx<T> acc[4][3];
+#pragma unroll
+        for (int s = 0; s < 4; s++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) acc[s][c] = {T(0), T(0)};
+        hop_pair<T, 4, RECON, ISIGN, 0>(a, h, n, acc);
+        hop_pair<T, 4, RECON, ISIGN, 1>(a, h, n, acc);
+        hop_pair<T, 4, RECON, ISIGN, 2>(a, h, n, acc);
+        hop_pair<T, 4, RECON, ISIGN, 3>(a, h, n, acc);
+        cx<T> xv[4][3];
+        load_spinor_any<T>(x, a.g.stride, h, xv);
+#pragma unroll
+        for (int s = 0; s < 4; s++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                acc[s][c].r = fma(coef, acc[s][c].r, xv[s][c].r);
+                acc[s][c].i = fma(coef, acc[s][c].i, xv[s][c].i);
+                nrm = fma(acc[s][c].r, acc[s][c].r, nrm);
+                nrm = fma(acc[s][c].i, acc[s][c].i, nrm);
+            }
+        Field<T>::store_spinor(a.res, a.g.stride, h, acc);
+    }
+    if (partials) block_sum_to<T>(partials, nrm);
+}
+
+template <typename T> struct XpayMinb;
+template <> struct XpayMinb<float> { static constexpr int r18 = 6, r12 = 6; };
+template <> struct XpayMinb<double> { static constexpr int r18 = 0, r12 = 0; };
+
+// Grid blocks of an xpay launch (the size `partials` must have).
+inline int xpay_blocks(const Geom &g) { return (g.Vh + 127) / 128; }
+
+template <typename T>
+cudaError_t launch_dslash_xpay_t(const Geom &g, int recon, const void *gauge, const void *psi, const void *x, T coef,
+                                 void *res, double *partials, int isign, int cb, cudaStream_t stream) {
+    DslashArgs<T> a;
+    a.g = g;
+    a.psi = static_cast<const typename VecOf<T>::S *>(psi);
+    a.res = static_cast<typename VecOf<T>::S *>(res);
+    a.gauge = static_cast<const char *>(gauge);
+    const int vec_bytes = sizeof(T) == 4 ? (recon == 18 ? 8 : 16) : 16;
+    a.link_block_bytes = (size_t)Field<T>::link_vecs(recon) * g.stride * vec_bytes;
+    a.pt = 1 - cb;
+    const dim3 grid(xpay_blocks(g));
+    const auto *xv = static_cast<const typename VecOf<T>::S *>(x);
+    constexpr int m18 = XpayMinb<T>::r18, m12 = XpayMinb<T>::r12;
+    if (recon == 18) {
+        if (isign > 0) dslash_xpay_kernel<T, 18, 1, m18><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
+        else dslash_xpay_kernel<T, 18, -1, m18><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
+    } else {
+        if (isign > 0) dslash_xpay_kernel<T, 12, 1, m12><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
+        else dslash_xpay_kernel<T, 12, -1, m12><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
+    }
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <typename T>
 void launch_minb(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, int minb, cudaStream_t s);
 

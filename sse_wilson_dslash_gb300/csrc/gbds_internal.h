@@ -36,6 +36,14 @@ cudaError_t launch_dslash_f64(const Geom &g, int recon, const void *gauge, const
                               void *res, int isign, int cb, int block, int variant, cudaStream_t stream);
 int dslash_variants(int prec);
 
+// res = x + coef * Dslash(psi) (4D; res and x on checkerboard 1-cb); if
+// partials != nullptr, partials[b] = sum of |res|^2 over launch block b
+// (there are (Vh + 127) / 128 blocks).
+cudaError_t launch_dslash_xpay_f32(const Geom &g, int recon, const void *gauge, const void *psi, const void *x,
+                                   float coef, void *res, double *partials, int isign, int cb, cudaStream_t stream);
+cudaError_t launch_dslash_xpay_f64(const Geom &g, int recon, const void *gauge, const void *psi, const void *x,
+                                   double coef, void *res, double *partials, int isign, int cb, cudaStream_t stream);
+
 // site0: first caller site held by the packed buffer (0 for a full lattice).
 cudaError_t launch_pack_spinor(const Geom &g, int prec, const void *psi_packed, const int *site_table,
                                int site0, int parity, void *spinor, cudaStream_t stream);

@@ -1,0 +1,518 @@
+// Even-odd preconditioned Wilson solver on one GPU.
+//
+//   M = 1 - kappa^2 D_eo D_oe   on checkerboard 0 (even sites), D = the
+//   Dslash of this library (D_oe: even source -> odd target, cb = 0;
+//   D_eo: odd source -> even target, cb = 1); M^+ is the same with isign = -1.
+//
+// CG on the normal equations A x = c, A = M^+ M, c = M^+ b.
+//   inner_prec 64: all-FP64 CG.
+//   inner_prec 32: FP32 CG (FP32 fields, FP32 arithmetic, per-block sums in
+//                  FP64) inside FP64 defect correction: the residual
+//                  r = c - A x, the solution update x += |r| e and all global
+//                  norms stay in FP64 on the GPU.
+// The reference library provides only D; a caller such as Chroma builds M and
+// its solvers around it (tests/dslashm_w.cc states D the same way).  Scalars
+// of the iteration (rr, pAp, alpha, beta) live in device memory and are
+// computed by the kernels themselves; the host reads rr only to test
+// convergence.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+
+#include "dslash_kernel.cuh"
+
+namespace gbds {
+namespace {
+
+struct Scalars {
+    double rr;        // |r|^2 of the running CG
+    double pAp;       // <p, A p> = |M p|^2
+    double alpha, beta;
+    double outer_rr;  // |r|^2 of the FP64 defect-correction residual
+    double norm;      // scratch result of a norm
+};
+
+constexpr int kThreads = 128;
+
+inline int blocks(const Geom &g) { return (g.Vh + kThreads - 1) / kThreads; }
+
+template <typename T> using SV = typename VecOf<T>::S;  // float4 / double2
+template <typename T> constexpr int nvec() { return sizeof(T) == 4 ? 6 : 12; }
+
+__device__ __forceinline__ float4 axpy_v(float a, float4 x, float4 y) {
+    return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+__device__ __forceinline__ double2 axpy_v(double a, double2 x, double2 y) {
+    return make_double2(fma(a, x.x, y.x), fma(a, x.y, y.y));
+}
+__device__ __forceinline__ float norm_v(float4 v) { return v.x * v.x + v.y * v.y + v.z * v.z + v.w * v.w; }
+__device__ __forceinline__ double norm_v(double2 v) { return v.x * v.x + v.y * v.y; }
+
+// x += alpha p;  r -= alpha Ap;  partial |r|^2
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cg_update(SV<T> *x, SV<T> *r, const SV<T> *__restrict__ p,
+                                                     const SV<T> *__restrict__ Ap, const Scalars *sc, int Vh, int stride,
+                                                     double *partials) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    T nrm = 0;
+    if (h < Vh) {
+        const T a = (T)sc->alpha;
+#pragma unroll
+        for (int k = 0; k < nvec<T>(); k++) {
+            const size_t i = (size_t)k * stride + h;
+            x[i] = axpy_v(a, p[i], x[i]);
+            const SV<T> rn = axpy_v(-a, Ap[i], r[i]);
+            r[i] = rn;
+            nrm += norm_v(rn);
+        }
+    }
+    block_sum_to<T>(partials, nrm);
+}
+
+// p = r + beta p
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cg_xpay(const SV<T> *__restrict__ r, SV<T> *p, const Scalars *sc, int Vh,
+                                                   int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+    const T b = (T)sc->beta;
+#pragma unroll
+    for (int k = 0; k < nvec<T>(); k++) {
+        const size_t i = (size_t)k * stride + h;
+        p[i] = axpy_v(b, p[i], r[i]);
+    }
+}
+
+// r = c - v; partial |r|^2  (FP64 defect residual)
+__global__ void __launch_bounds__(kThreads) xmy_norm(const double2 *__restrict__ c, const double2 *__restrict__ v,
+                                                    double2 *r, int Vh, int stride, double *partials) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    double nrm = 0;
+    if (h < Vh) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+            const size_t i = (size_t)k * stride + h;
+            const double2 d = make_double2(c[i].x - v[i].x, c[i].y - v[i].y);
+            r[i] = d;
+            nrm += norm_v(d);
+        }
+    }
+    block_sum_to<double>(partials, nrm);
+}
+
+// partial |v|^2, and optionally dst = v
+template <typename T>
+__global__ void __launch_bounds__(kThreads) norm_copy(const SV<T> *__restrict__ v, SV<T> *dst, SV<T> *dst2, int Vh,
+                                                     int stride, double *partials) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    T nrm = 0;
+    if (h < Vh) {
+#pragma unroll
+        for (int k = 0; k < nvec<T>(); k++) {
+            const size_t i = (size_t)k * stride + h;
+            const SV<T> a = v[i];
+            if (dst) dst[i] = a;
+            if (dst2) dst2[i] = a;
+            nrm += norm_v(a);
+        }
+    }
+    block_sum_to<T>(partials, nrm);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) zero_field(SV<T> *v, int Vh, int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+    const SV<T> z = {};
+#pragma unroll
+    for (int k = 0; k < nvec<T>(); k++) v[(size_t)k * stride + h] = z;
+}
+
+// r32 = r64 / sqrt(outer_rr);  p32 = r32
+__global__ void __launch_bounds__(kThreads) demote_residual(const double2 *__restrict__ r64, float4 *r32, float4 *p32,
+                                                           const Scalars *sc, int Vh, int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+    const double s = 1.0 / sqrt(sc->outer_rr);
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const double2 a = r64[(size_t)(2 * k) * stride + h], b = r64[(size_t)(2 * k + 1) * stride + h];
+        const float4 f = make_float4((float)(a.x * s), (float)(a.y * s), (float)(b.x * s), (float)(b.y * s));
+        r32[(size_t)k * stride + h] = f;
+        p32[(size_t)k * stride + h] = f;
+    }
+}
+
+// x64 += sqrt(outer_rr) * e32
+__global__ void __launch_bounds__(kThreads) promote_update(const float4 *__restrict__ e32, double2 *x64,
+                                                          const Scalars *sc, int Vh, int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+    const double s = sqrt(sc->outer_rr);
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float4 e = e32[(size_t)k * stride + h];
+        double2 &a = x64[(size_t)(2 * k) * stride + h];
+        double2 &b = x64[(size_t)(2 * k + 1) * stride + h];
+        a.x = fma(s, (double)e.x, a.x);
+        a.y = fma(s, (double)e.y, a.y);
+        b.x = fma(s, (double)e.z, b.x);
+        b.y = fma(s, (double)e.w, b.y);
+    }
+}
+
+enum FinishMode { kAlpha = 0, kBeta = 1, kSetRR = 2, kOuterRR = 3, kNorm = 4 };
+
+// Deterministic sum of the block partials (fixed order), then the scalar step.
+__global__ void __launch_bounds__(1024) finish(const double *partials, int n, Scalars *sc, int mode) {
+    __shared__ double buf[1024];
+    double t = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) t += partials[i];
+    buf[threadIdx.x] = t;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) buf[threadIdx.x] += buf[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double sum = buf[0];
+    switch (mode) {
+    case kAlpha: sc->pAp = sum; sc->alpha = sum > 0 ? sc->rr / sum : 0.0; break;
+    case kBeta: sc->beta = sc->rr > 0 ? sum / sc->rr : 0.0; sc->rr = sum; break;
+    case kSetRR: sc->rr = sum; break;
+    case kOuterRR: sc->outer_rr = sum; break;
+    default: sc->norm = sum; break;
+    }
+}
+
+__global__ void f64_to_f32(const double *__restrict__ a, float *b, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+}  // namespace
+}  // namespace gbds
+
+using namespace gbds;
+
+struct gbds_solver_s {
+    Geom g;
+    gbds_solver_params prm;
+    void *gauge64 = nullptr;  // FP64, recon 18
+    void *gauge32 = nullptr;  // FP32, inner recon
+    // FP64 fields (checkerboard 0 except t64: checkerboard 1)
+    void *b64 = nullptr, *c64 = nullptr, *x64 = nullptr, *r64 = nullptr, *p64 = nullptr, *Ap64 = nullptr,
+         *Mp64 = nullptr, *t64 = nullptr;
+    // FP32 inner fields
+    void *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *Mp32 = nullptr, *t32 = nullptr;
+    double *partials = nullptr;
+    Scalars *sc = nullptr;    // device
+    Scalars *hsc = nullptr;   // pinned host copy
+    bool have_gauge = false;
+};
+
+namespace {
+
+// Dslash launches through the precision-specific entry points (the kernels are
+// instantiated once, in dslash_f32.cu / dslash_f64.cu).
+template <typename T>
+cudaError_t dslash(const Geom &g, int recon, const void *gauge, const void *psi, void *res, int isign, int cb,
+                   int block, int variant, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4) return launch_dslash_f32(g, recon, gauge, psi, res, isign, cb, block, variant, st);
+    else return launch_dslash_f64(g, recon, gauge, psi, res, isign, cb, block, variant, st);
+}
+
+template <typename T>
+cudaError_t dslash_xpay(const Geom &g, int recon, const void *gauge, const void *psi, const void *x, T coef, void *res,
+                        double *partials, int isign, int cb, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4) return launch_dslash_xpay_f32(g, recon, gauge, psi, x, coef, res, partials, isign, cb, st);
+    else return launch_dslash_xpay_f64(g, recon, gauge, psi, x, coef, res, partials, isign, cb, st);
+}
+
+cudaError_t finish_on(gbds_solver s, int mode, cudaStream_t st) {
+    finish<<<1, 1024, 0, st>>>(s->partials, blocks(s->g), s->sc, mode);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// out_e = in_e - kappa^2 D_eo(isign) D_oe(isign) in_e  (partials: |out|^2)
+template <typename T>
+cudaError_t apply_M(gbds_solver s, const void *gauge, int recon, const void *in, void *tmp, void *out, int isign,
+                    double *partials, cudaStream_t st) {
+    const Geom &g = s->g;
+    const double k2 = s->prm.kappa * s->prm.kappa;
+    const int variant = (sizeof(T) == 4 && recon == 18) ? 1 : 0;
+    const int block = (sizeof(T) == 4 && recon == 12) ? 64 : 128;
+    cudaError_t e = dslash<T>(g, recon, gauge, in, tmp, isign, 0, block, variant, st);
+    if (e != cudaSuccess) return e;
+    return dslash_xpay<T>(g, recon, gauge, tmp, in, (T)(-k2), out, partials, isign, 1, st);
+}
+
+cudaError_t read_scalars(gbds_solver s, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(s->hsc, s->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
+// CG on A = M^+ M with x, r, p prepared (x = 0, r = p = rhs, sc->rr = |rhs|^2).
+// Stops when rr <= target_rr or after max_iter iterations.
+template <typename T>
+cudaError_t cg(gbds_solver s, const void *gauge, int recon, void *x, void *r, void *p, void *Ap, void *Mp, void *t,
+               double target_rr, int max_iter, int *iters, cudaStream_t st) {
+    const Geom &g = s->g;
+    const int nb = blocks(g);
+    const int check_every = sizeof(T) == 4 ? 4 : 1;
+    cudaError_t e = cudaSuccess;
+    int k = 0;
+    while (k < max_iter) {
+        e = apply_M<T>(s, gauge, recon, p, t, Mp, +1, s->partials, st);
+        if (e == cudaSuccess) e = finish_on(s, kAlpha, st);
+        if (e == cudaSuccess) e = apply_M<T>(s, gauge, recon, Mp, t, Ap, -1, nullptr, st);
+        if (e == cudaSuccess) {
+            cg_update<T><<<nb, kThreads, 0, st>>>(static_cast<SV<T> *>(x), static_cast<SV<T> *>(r),
+                                                   static_cast<const SV<T> *>(p), static_cast<const SV<T> *>(Ap), s->sc,
+                                                   g.Vh, g.stride, s->partials);
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = finish_on(s, kBeta, st);
+        if (e == cudaSuccess) {
+            cg_xpay<T><<<nb, kThreads, 0, st>>>(static_cast<const SV<T> *>(r), static_cast<SV<T> *>(p), s->sc, g.Vh,
+                                                 g.stride);
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e != cudaSuccess) break;
+        k++;
+        if (k % check_every == 0 || k == max_iter) {
+            e = read_scalars(s, st);
+            if (e != cudaSuccess) break;
+            if (!(s->hsc->rr > target_rr)) break;  // converged (or NaN: stop)
+        }
+    }
+    *iters = k;
+    return e;
+}
+
+template <typename T>
+cudaError_t norm_into(gbds_solver s, const void *v, void *dst, void *dst2, int mode, cudaStream_t st) {
+    norm_copy<T><<<blocks(s->g), kThreads, 0, st>>>(static_cast<const SV<T> *>(v), static_cast<SV<T> *>(dst),
+                                                     static_cast<SV<T> *>(dst2), s->g.Vh, s->g.stride, s->partials);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? finish_on(s, mode, st) : e;
+}
+
+template <typename T>
+cudaError_t zero(gbds_solver s, void *v, cudaStream_t st) {
+    zero_field<T><<<blocks(s->g), kThreads, 0, st>>>(static_cast<SV<T> *>(v), s->g.Vh, s->g.stride);
+    count_launch();
+    return cudaGetLastError();
+}
+
+void release(gbds_solver s) {
+    void *bufs[] = {s->gauge64, s->gauge32, s->b64, s->c64, s->x64, s->r64, s->p64, s->Ap64, s->Mp64, s->t64,
+                    s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32, s->partials, s->sc};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    if (s->hsc) cudaFreeHost(s->hsc);
+}
+
+}  // namespace
+
+extern "C" int gbds_solver_create(gbds_solver *out, const int dims[4], const gbds_solver_params *p) {
+    if (!out || !p) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL argument");
+    *out = nullptr;
+    if (p->inner_prec != 64 && p->inner_prec != 32)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "inner_prec must be 64 or 32");
+    if (p->inner_recon != 18 && p->inner_recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "inner_recon must be 18 or 12");
+    if (!(p->tol > 0) || p->max_iter <= 0 || !(p->kappa > 0))
+        return set_error(GBDS_ERROR_INVALID_VALUE, "tol, max_iter and kappa must be positive");
+    Geom g;
+    int rc = make_geom(dims, 4, &g);
+    if (rc != GBDS_SUCCESS) return rc;
+    gbds_solver s = new (std::nothrow) gbds_solver_s;
+    if (!s) return set_error(GBDS_ERROR_OUT_OF_MEMORY, "host allocation failed");
+    s->g = g;
+    s->prm = *p;
+    if (!(s->prm.inner_tol > 0 && s->prm.inner_tol < 1)) s->prm.inner_tol = 1e-5;
+    const size_t f64 = spinor_bytes(g, 64), f32 = spinor_bytes(g, 32);
+    cudaError_t e = cudaSuccess;
+    void **d64[] = {&s->b64, &s->c64, &s->x64, &s->r64, &s->p64, &s->Ap64, &s->Mp64, &s->t64};
+    for (void **b : d64)
+        if (e == cudaSuccess) e = cudaMalloc(b, f64);
+    if (p->inner_prec == 32) {
+        void **d32[] = {&s->e32, &s->r32, &s->p32, &s->Ap32, &s->Mp32, &s->t32};
+        for (void **b : d32)
+            if (e == cudaSuccess) e = cudaMalloc(b, f32);
+        if (e == cudaSuccess) e = cudaMalloc(&s->gauge32, gauge_bytes(g, 32, p->inner_recon));
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&s->gauge64, gauge_bytes(g, 64, 18));
+    if (e == cudaSuccess) e = cudaMalloc(&s->partials, sizeof(double) * (size_t)blocks(g));
+    if (e == cudaSuccess) e = cudaMalloc(&s->sc, sizeof(Scalars));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->hsc, sizeof(Scalars));
+    if (e != cudaSuccess) {
+        release(s);
+        delete s;
+        return cuda_error(e, "gbds_solver_create");
+    }
+    *out = s;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_solver_destroy(gbds_solver s) {
+    if (!s) return GBDS_SUCCESS;
+    cudaDeviceSynchronize();
+    release(s);
+    delete s;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_solver_set_gauge(gbds_solver s, const double *u_packed, void *stream) {
+    if (!s) return set_error(GBDS_ERROR_NOT_INITIALIZED, "solver is NULL");
+    if (!u_packed || (reinterpret_cast<uintptr_t>(u_packed) & 15u))
+        return set_error(GBDS_ERROR_INVALID_VALUE, "u_packed must be a 16-byte aligned device pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_pack_gauge(s->g, 64, 18, u_packed, nullptr, s->gauge64, st);
+    if (e == cudaSuccess && s->prm.inner_prec == 32) {
+        const size_t n = (size_t)s->g.V * 72;
+        float *tmp = nullptr;
+        e = cudaMallocAsync(reinterpret_cast<void **>(&tmp), n * sizeof(float), st);
+        if (e == cudaSuccess) {
+            f64_to_f32<<<1024, 256, 0, st>>>(u_packed, tmp, n);
+            count_launch();
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = launch_pack_gauge(s->g, 32, s->prm.inner_recon, tmp, nullptr, s->gauge32, st);
+            cudaFreeAsync(tmp, st);
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_solver_set_gauge");
+    s->have_gauge = true;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_solver_apply(gbds_solver s, const double *x_packed, double *y_packed, int dagger, void *stream) {
+    if (!s) return set_error(GBDS_ERROR_NOT_INITIALIZED, "solver is NULL");
+    if (!s->have_gauge) return set_error(GBDS_ERROR_NOT_INITIALIZED, "gbds_solver_set_gauge has not been called");
+    if (!x_packed || !y_packed) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL field pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_pack_spinor(s->g, 64, x_packed, nullptr, 0, 0, s->b64, st);
+    if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->b64, s->t64, s->Mp64, dagger ? -1 : 1, nullptr, st);
+    if (e == cudaSuccess) e = launch_unpack_spinor(s->g, 64, s->Mp64, nullptr, 0, 0, y_packed, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "gbds_solver_apply");
+}
+
+extern "C" int gbds_solver_solve(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats,
+                                 void *stream) {
+    if (!s) return set_error(GBDS_ERROR_NOT_INITIALIZED, "solver is NULL");
+    if (!s->have_gauge) return set_error(GBDS_ERROR_NOT_INITIALIZED, "gbds_solver_set_gauge has not been called");
+    if (!b_packed || !x_packed) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL field pointer");
+    if ((reinterpret_cast<uintptr_t>(b_packed) | reinterpret_cast<uintptr_t>(x_packed)) & 15u)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const auto t0 = std::chrono::steady_clock::now();
+    gbds_solver_stats out = {};
+    const Geom &g = s->g;
+    const double tol2 = s->prm.tol * s->prm.tol;
+    // b, c = M^+ b, |c|^2
+    cudaError_t e = launch_pack_spinor(g, 64, b_packed, nullptr, 0, 0, s->b64, st);
+    if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->b64, s->t64, s->c64, -1, s->partials, st);
+    if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
+    if (e == cudaSuccess) e = zero<double>(s, s->x64, st);
+    if (e == cudaSuccess) e = read_scalars(s, st);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");
+    const double c2 = s->hsc->outer_rr;
+    double outer_rr = c2;
+    int total = 0;
+    if (c2 > 0) {
+        if (s->prm.inner_prec == 64) {
+            // all-FP64 CG: r = p = c
+            e = norm_into<double>(s, s->c64, s->r64, s->p64, kSetRR, st);
+            int it = 0;
+            if (e == cudaSuccess)
+                e = cg<double>(s, s->gauge64, 18, s->x64, s->r64, s->p64, s->Ap64, s->Mp64, s->t64, tol2 * c2,
+                               s->prm.max_iter, &it, st);
+            total = it;
+            out.cycles = 1;
+        } else {
+            // FP64 defect correction around FP32 CG; r64 starts as c.
+            e = norm_into<double>(s, s->c64, s->r64, nullptr, kOuterRR, st);
+            while (e == cudaSuccess && outer_rr > tol2 * c2 && total < s->prm.max_iter) {
+                const int nb = blocks(g);
+                demote_residual<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->r64), static_cast<float4 *>(s->r32),
+                                                         static_cast<float4 *>(s->p32), s->sc, g.Vh, g.stride);
+                count_launch();
+                e = cudaGetLastError();
+                if (e == cudaSuccess) e = zero<float>(s, s->e32, st);
+                if (e == cudaSuccess) e = norm_into<float>(s, s->r32, nullptr, nullptr, kSetRR, st);
+                if (e != cudaSuccess) break;
+                // inner target: the requested reduction, but no further than the outer goal needs
+                double delta = s->prm.inner_tol;
+                const double need = 0.5 * s->prm.tol * std::sqrt(c2 / outer_rr);
+                if (need > delta) delta = need;
+                int it = 0;
+                e = cg<float>(s, s->gauge32, s->prm.inner_recon, s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32,
+                              delta * delta, s->prm.max_iter - total, &it, st);
+                total += it;
+                out.cycles++;
+                if (e != cudaSuccess) break;
+                promote_update<<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->e32), static_cast<double2 *>(s->x64),
+                                                        s->sc, g.Vh, g.stride);
+                count_launch();
+                e = cudaGetLastError();
+                // true residual r = c - A x in FP64
+                if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->x64, s->t64, s->Mp64, +1, nullptr, st);
+                if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->Mp64, s->t64, s->Ap64, -1, nullptr, st);
+                if (e == cudaSuccess) {
+                    xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->c64), static_cast<const double2 *>(s->Ap64),
+                                                      static_cast<double2 *>(s->r64), g.Vh, g.stride, s->partials);
+                    count_launch();
+                    e = cudaGetLastError();
+                }
+                if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
+                if (e == cudaSuccess) e = read_scalars(s, st);
+                if (e != cudaSuccess) break;
+                const double prev = outer_rr;
+                outer_rr = s->hsc->outer_rr;
+                if (!(outer_rr < prev)) break;  // no progress (or NaN): stop
+            }
+        }
+    }
+    if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");
+    // FP64 checks: |c - A x| / |c| and |b - M x| / |b|
+    e = apply_M<double>(s, s->gauge64, 18, s->x64, s->t64, s->Mp64, +1, nullptr, st);
+    if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->Mp64, s->t64, s->Ap64, -1, nullptr, st);
+    const int nb = blocks(g);
+    if (e == cudaSuccess) {
+        xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->c64), static_cast<const double2 *>(s->Ap64),
+                                          static_cast<double2 *>(s->r64), g.Vh, g.stride, s->partials);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
+    if (e == cudaSuccess) e = read_scalars(s, st);
+    const double final_rr = s->hsc->outer_rr;
+    if (e == cudaSuccess) {
+        xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->b64), static_cast<const double2 *>(s->Mp64),
+                                          static_cast<double2 *>(s->p64), g.Vh, g.stride, s->partials);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = finish_on(s, kNorm, st);
+    if (e == cudaSuccess) e = norm_into<double>(s, s->b64, nullptr, nullptr, kOuterRR, st);
+    if (e == cudaSuccess) e = read_scalars(s, st);
+    if (e == cudaSuccess) e = launch_unpack_spinor(g, 64, s->x64, nullptr, 0, 0, x_packed, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");
+    out.iterations = total;
+    out.residual = c2 > 0 ? std::sqrt(final_rr / c2) : 0.0;
+    out.true_residual = s->hsc->outer_rr > 0 ? std::sqrt(s->hsc->norm / s->hsc->outer_rr) : 0.0;
+    out.converged = out.residual <= s->prm.tol ? 1 : 0;
+    out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = out;
+    return GBDS_SUCCESS;
+}
