@@ -241,6 +241,36 @@ def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None):
     return res
 
 
+def multi_rhs_variants(torch, steps, peak):
+    """Several right-hand sides on one 24^3x48 gauge field: FP32 and BF16
+    spinor storage, 18-real links; GFLOP/s counts 1320 flop per site and
+    right-hand side."""
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims = (24, 24, 24, 48)
+    V = dims[0] * dims[1] * dims[2] * dims[3]
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    u = su3_links(V * 4, gen, torch).float().reshape(-1)
+    out = {}
+    for fmt in ("native", "bf16"):
+        for nrhs in (1, 4, 8, 16, 32):
+            op = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
+            gauge = op.pack_gauge(u)
+            psi = torch.randn(nrhs * V * 24, dtype=torch.float32, device="cuda", generator=gen)
+            srcs = [op.pack_spinor(psi, 0), op.pack_spinor(psi, 1)]
+            del psi
+            outs = [op.new_spinor(), op.new_spinor()]
+            ms = time_device(op, gauge, srcs, outs, max(10, steps // max(1, nrhs // 4)), 3, torch)
+            sites = op.volume_cb * nrhs
+            gbs = op.bytes_per_site * sites / (ms * 1e6)
+            out[f"{'f32' if fmt == 'native' else 'bf16'}_nrhs{nrhs}"] = {
+                "ms": ms, "gflops": 1320 * sites / (ms * 1e6), "gbs": gbs, "roofline_frac": gbs / peak,
+                "ms_per_rhs": ms / nrhs, "bytes_per_site_rhs": op.bytes_per_site}
+            del gauge, srcs, outs
+            op.close()
+            torch.cuda.empty_cache()
+    return out
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -382,7 +412,12 @@ def run_gb300(args):
     gauge = op.pack_gauge(u)
     srcs = [op.pack_spinor(psi, 0), op.pack_spinor(psi, 1)]
     outs = [op.new_spinor(), op.new_spinor()]
-    tuning = op.autotune(gauge, srcs[0], outs[1])
+    if args.tuning:
+        blk, var = (int(v) for v in args.tuning.split(","))
+        op.set_tuning(blk, var)
+        tuning = op.tuning()
+    else:
+        tuning = op.autotune(gauge, srcs[0], outs[1])
     stream = torch.cuda.current_stream()
     combos = [(1, 0), (-1, 1), (-1, 0), (1, 1)]
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
@@ -515,6 +550,7 @@ def run_gb300(args):
         variants["3d_24x24x24x48_f32_recon12"] = device_variant(DIMS_3D, 3, 32, 12, vsteps, 5, torch)
         for v in variants.values():
             v["roofline_frac"] = v["gbs"] / peak
+        variants["multi_rhs_24x24x24x48"] = multi_rhs_variants(torch, vsteps, peak)
 
     solver = None
     if not args.no_solver:
@@ -557,6 +593,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true")
+    ap.add_argument("--tuning", default=None,
+                    help="block,variant of the headline kernel instead of autotuning (for profiling runs)")
     ap.add_argument("--dims", default=None,
                     help="Lx,Ly,Lz,Lt of the 4D workload (default 32,32,32,64; smaller cases are for profiling)")
     args = ap.parse_args()

@@ -86,6 +86,22 @@ typedef struct gbds_op_s *gbds_op;
 int gbds_op_create(gbds_op *op, const int dims[4], int nd, int prec, int recon);
 int gbds_op_destroy(gbds_op op);
 
+/* Storage formats of spinor fields (gbds_op_create_ex). */
+#define GBDS_SPINOR_NATIVE 0   /* FP32 float4 or FP64 double2, as prec        */
+#define GBDS_SPINOR_BF16 1     /* 24 bfloat16 per spinor (48 B)                */
+#define GBDS_SPINOR_F16_NORM 2 /* 24 half scaled by a per-spinor float norm (52 B) */
+
+/* As gbds_op_create, for nrhs right-hand sides per site (1, 2, 4, 8, 16 or
+ * 32) and a spinor storage format.  nrhs > 1 or a 16-bit format needs
+ * prec 32 and nd 4; arithmetic is FP32.  A field then holds nrhs spinors per
+ * site, element (k, h, r) at k*stride*nrhs + h*nrhs + r (k: 16-byte component,
+ * h: site, r: right-hand side), half formats followed by one float norm per
+ * (h, r).  pack/unpack take FP32 packed arrays [nrhs][V][4][3][2]; the gauge
+ * field is the FP32 one of gbds_op_pack_gauge, shared by all right-hand
+ * sides, so each link is read once per site for all nrhs of them. */
+int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int prec, int recon, int nrhs, int format);
+int gbds_op_nrhs(gbds_op op);
+
 /* Caller site layout for pack/unpack: site_table[i] = caller linear index of
  * internal site i (i = p*Vh + h, internal order above), n = V entries, a
  * permutation of [0, V).  NULL (or the identity) selects the canonical

@@ -90,10 +90,20 @@ extern "C" const char *gbds_get_last_error(void) { return g_last_error.c_str(); 
 extern "C" long long gbds_kernel_launch_count(void) { return g_launches.load(); }
 
 extern "C" int gbds_op_create(gbds_op *op, const int dims[4], int nd, int prec, int recon) {
+    return gbds_op_create_ex(op, dims, nd, prec, recon, 1, GBDS_SPINOR_NATIVE);
+}
+
+extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int prec, int recon, int nrhs, int format) {
     if (!op) return set_error(GBDS_ERROR_INVALID_VALUE, "op is NULL");
     *op = nullptr;
     if (prec != 32 && prec != 64) return set_error(GBDS_ERROR_INVALID_VALUE, "prec must be 32 or 64");
     if (recon != 18 && recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "recon must be 18 or 12");
+    if (nrhs != 1 && nrhs != 2 && nrhs != 4 && nrhs != 8 && nrhs != 16 && nrhs != 32)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "nrhs must be 1, 2, 4, 8, 16 or 32");
+    if (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_BF16 && format != GBDS_SPINOR_F16_NORM)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "unknown spinor format");
+    if ((nrhs > 1 || format != GBDS_SPINOR_NATIVE) && (prec != 32 || nd != 4))
+        return set_error(GBDS_ERROR_UNSUPPORTED, "several right-hand sides and 16-bit spinors need prec 32 and nd 4");
     Geom g;
     int rc = make_geom(dims, nd, &g);
     if (rc != GBDS_SUCCESS) return rc;
@@ -108,6 +118,8 @@ extern "C" int gbds_op_create(gbds_op *op, const int dims[4], int nd, int prec, 
     // FP64 (FP64-issue bound) is insensitive.
     o->block = (prec == 32 && recon == 12) ? 64 : 128;
     o->variant = (prec == 32 && recon == 18) ? 1 : 0;
+    o->nrhs = nrhs;
+    o->format = format;
     o->d_site_table = nullptr;
     *op = o;
     return GBDS_SUCCESS;
@@ -150,7 +162,15 @@ extern "C" int gbds_op_set_layout(gbds_op op, const int *site_table, int n) {
 
 extern "C" int gbds_op_is_canonical(gbds_op op) { return op && op->d_site_table == nullptr; }
 
-extern "C" size_t gbds_op_spinor_bytes(gbds_op op) { return op ? spinor_bytes(op->g, op->prec) : 0; }
+static bool generic(gbds_op op) { return op->nrhs > 1 || op->format != GBDS_SPINOR_NATIVE; }
+
+extern "C" size_t gbds_op_spinor_bytes(gbds_op op) {
+    if (!op) return 0;
+    if (generic(op)) return (size_t)gen_spinor_bytes(op->format) * op->g.stride * op->nrhs;
+    return spinor_bytes(op->g, op->prec);
+}
+
+extern "C" int gbds_op_nrhs(gbds_op op) { return op ? op->nrhs : 0; }
 
 extern "C" size_t gbds_op_gauge_bytes(gbds_op op) { return op ? gauge_bytes(op->g, op->prec, op->recon) : 0; }
 
@@ -249,8 +269,15 @@ extern "C" int gbds_op_pack_spinor(gbds_op op, const void *psi_packed, int parit
     if (!psi_packed || !spinor) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL field pointer");
     if (parity != 0 && parity != 1) return set_error(GBDS_ERROR_INVALID_VALUE, "parity must be 0 or 1");
     if (!aligned16(psi_packed) || !aligned16(spinor)) return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
-    cudaError_t e = launch_pack_spinor(op->g, op->prec, psi_packed, op->d_site_table, 0, parity, spinor,
-                                       static_cast<cudaStream_t>(stream));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (generic(op)) {
+        const float *src = static_cast<const float *>(psi_packed);
+        cudaError_t e = op->format == GBDS_SPINOR_NATIVE
+                            ? launch_pack_gen_f32(op->g, op->nrhs, src, op->d_site_table, parity, spinor, st)
+                            : launch_pack_gen_half(op->format, op->g, op->nrhs, src, op->d_site_table, parity, spinor, st);
+        return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_spinor");
+    }
+    cudaError_t e = launch_pack_spinor(op->g, op->prec, psi_packed, op->d_site_table, 0, parity, spinor, st);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_spinor");
 }
 
@@ -259,8 +286,15 @@ extern "C" int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity,
     if (!psi_packed || !spinor) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL field pointer");
     if (parity != 0 && parity != 1) return set_error(GBDS_ERROR_INVALID_VALUE, "parity must be 0 or 1");
     if (!aligned16(psi_packed) || !aligned16(spinor)) return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
-    cudaError_t e = launch_unpack_spinor(op->g, op->prec, spinor, op->d_site_table, 0, parity, psi_packed,
-                                         static_cast<cudaStream_t>(stream));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (generic(op)) {
+        float *dst = static_cast<float *>(psi_packed);
+        cudaError_t e = op->format == GBDS_SPINOR_NATIVE
+                            ? launch_unpack_gen_f32(op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st)
+                            : launch_unpack_gen_half(op->format, op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st);
+        return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "unpack_spinor");
+    }
+    cudaError_t e = launch_unpack_spinor(op->g, op->prec, spinor, op->d_site_table, 0, parity, psi_packed, st);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "unpack_spinor");
 }
 
@@ -273,6 +307,13 @@ extern "C" int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, vo
     if (!aligned16(gauge) || !aligned16(psi) || !aligned16(res))
         return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (generic(op)) {
+        cudaError_t e = op->format == GBDS_SPINOR_NATIVE
+                            ? launch_gen_f32(op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f, nullptr, s)
+                            : launch_gen_half(op->format, op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr,
+                                              0.f, nullptr, s);
+        return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
+    }
     cudaError_t e = op->prec == 32 ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)
                                    : launch_dslash_f64(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");

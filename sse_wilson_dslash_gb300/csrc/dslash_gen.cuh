@@ -1,0 +1,203 @@
+// Generalised Dslash: several right-hand sides per site and reduced-precision
+// spinor storage, FP32 arithmetic, FP32 links (18 or 12 reals).
+//
+// Spinor field of one checkerboard with NRHS right-hand sides, element
+// (component k, site h, rhs r) at  k * CS + h * NRHS + r,  CS = stride * NRHS:
+// the right-hand-side index runs fastest, so the NRHS lanes that work on one
+// site read one link (a broadcast load) and consecutive lanes read
+// consecutive spinor words.  With NRHS right-hand sides a site's 2*nd links
+// are read once for all of them: compulsory bytes per site and rhs are
+// 2 s + 2 nd g / NRHS (s, g = spinor, link bytes).
+//
+// Storage formats (SpinorIO):
+//   F32   6 float4 per spinor (96 B)
+//   BF16  3 uint4 per spinor, 24 bfloat16 (48 B)
+//   F16N  3 uint4 per spinor, 24 half scaled by a per-spinor float norm
+//         stored after the components (48 + 4 B): value = half * norm,
+//         norm = max |component|.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "dslash_kernel.cuh"
+
+namespace gbds {
+
+enum SpinorFormat { kFmtNative = 0, kFmtBF16 = 1, kFmtF16N = 2 };
+
+// Load/store of one spinor at element index i, component stride cs (elements).
+template <int FMT> struct Sio;
+
+template <>
+struct Sio<kFmtNative> {
+    static constexpr int kBytes = 96;
+    __device__ __forceinline__ static void load(const char *base, size_t cs, size_t i, cx<float> (&s)[4][3]) {
+        const float4 *p = reinterpret_cast<const float4 *>(base);
+        float v[24];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const float4 q = __ldg(p + k * cs + i);
+            v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 12; j++) s[j / 3][j % 3] = {v[2 * j], v[2 * j + 1]};
+    }
+    __device__ __forceinline__ static void store(char *base, size_t cs, size_t i, const cx<float> (&s)[4][3]) {
+        float4 *p = reinterpret_cast<float4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const cx<float> a = s[(2 * k) / 3][(2 * k) % 3], b = s[(2 * k + 1) / 3][(2 * k + 1) % 3];
+            __stcs(p + k * cs + i, make_float4(a.r, a.i, b.r, b.i));
+        }
+    }
+};
+
+template <>
+struct Sio<kFmtBF16> {
+    static constexpr int kBytes = 48;
+    __device__ __forceinline__ static void load(const char *base, size_t cs, size_t i, cx<float> (&s)[4][3]) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint4 q = __ldg(p + k * cs + i);
+            const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int c = 0; c < 4; c++) {  // one complex per 32-bit word
+                const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162 *>(&w[c]);
+                const float2 f = __bfloat1622float2(b);
+                const int j = 4 * k + c;
+                s[j / 3][j % 3] = {f.x, f.y};
+            }
+        }
+    }
+    __device__ __forceinline__ static void store(char *base, size_t cs, size_t i, const cx<float> (&s)[4][3]) {
+        uint4 *p = reinterpret_cast<uint4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            unsigned w[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int j = 4 * k + c;
+                const __nv_bfloat162 b = __floats2bfloat162_rn(s[j / 3][j % 3].r, s[j / 3][j % 3].i);
+                w[c] = *reinterpret_cast<const unsigned *>(&b);
+            }
+            __stcs(p + k * cs + i, make_uint4(w[0], w[1], w[2], w[3]));
+        }
+    }
+};
+
+template <>
+struct Sio<kFmtF16N> {
+    static constexpr int kBytes = 52;
+    // norms follow the three uint4 component arrays
+    __device__ __forceinline__ static const float *norms(const char *base, size_t cs) {
+        return reinterpret_cast<const float *>(base + 3 * 16 * cs);
+    }
+    __device__ __forceinline__ static void load(const char *base, size_t cs, size_t i, cx<float> (&s)[4][3]) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(base);
+        const float nrm = __ldg(norms(base, cs) + i);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint4 q = __ldg(p + k * cs + i);
+            const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const __half2 b = *reinterpret_cast<const __half2 *>(&w[c]);
+                const float2 f = __half22float2(b);
+                const int j = 4 * k + c;
+                s[j / 3][j % 3] = {f.x * nrm, f.y * nrm};
+            }
+        }
+    }
+    __device__ __forceinline__ static void store(char *base, size_t cs, size_t i, const cx<float> (&s)[4][3]) {
+        float m = 0.f;
+#pragma unroll
+        for (int j = 0; j < 12; j++) m = fmaxf(m, fmaxf(fabsf(s[j / 3][j % 3].r), fabsf(s[j / 3][j % 3].i)));
+        const float inv = m > 0.f ? 1.f / m : 0.f;
+        uint4 *p = reinterpret_cast<uint4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            unsigned w[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int j = 4 * k + c;
+                const __half2 b = __floats2half2_rn(s[j / 3][j % 3].r * inv, s[j / 3][j % 3].i * inv);
+                w[c] = *reinterpret_cast<const unsigned *>(&b);
+            }
+            __stcs(p + k * cs + i, make_uint4(w[0], w[1], w[2], w[3]));
+        }
+        __stcs(reinterpret_cast<float *>(base + 3 * 16 * cs) + i, m);
+    }
+};
+
+struct GenArgs {
+    Geom g;
+    const char *psi;           // source checkerboard
+    char *res;                 // target checkerboard
+    const char *gauge;         // FP32 links, both checkerboards
+    size_t link_block_bytes;   // one (parity, mu) block
+    size_t cs;                 // component stride of the spinor arrays (elements) = stride * NRHS
+    int pt;                    // target parity
+    // xpay epilogue: res = x + coef * D psi, |res|^2 partials
+    const char *x;
+    float coef;
+    double *partials;
+};
+
+template <int FMT, int RECON, int ISIGN, int NRHS, int MU>
+__device__ __forceinline__ void gen_hop_pair(const GenArgs &a, int h, int r, const Nbr &n, cx<float> (&acc)[4][3]) {
+    const int ps = 1 - a.pt;
+    cx<float> s[4][3], hs[2][3], w[2][3], U[3][3];
+    Sio<FMT>::load(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, s);
+    Field<float>::template load_link<RECON>(a.gauge + (size_t)(a.pt * 4 + MU) * a.link_block_bytes, a.g.stride, h, U);
+    project<MU, ISIGN>(s, hs);
+    su3_mul<false>(U, hs, w);
+    reconstruct<MU, ISIGN>(acc, w);
+    Sio<FMT>::load(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, s);
+    Field<float>::template load_link<RECON>(a.gauge + (size_t)(ps * 4 + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
+    project<MU, -ISIGN>(s, hs);
+    su3_mul<true>(U, hs, w);
+    reconstruct<MU, -ISIGN>(acc, w);
+}
+
+// One thread per (site, rhs); 4D.  EPI = 1 adds the xpay epilogue.
+template <int FMT, int RECON, int ISIGN, int NRHS, int EPI>
+__global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = t / NRHS, r = t % NRHS;
+    float nrm = 0.f;
+    if (h < a.g.Vh) {
+        Nbr n;
+        neighbours<4>(a.g, h, a.pt, n);
+        cx<float> acc[4][3];
+#pragma unroll
+        for (int s = 0; s < 4; s++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) acc[s][c] = {0.f, 0.f};
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 0>(a, h, r, n, acc);
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 1>(a, h, r, n, acc);
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 2>(a, h, r, n, acc);
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 3>(a, h, r, n, acc);
+        const size_t i = (size_t)h * NRHS + r;
+        if constexpr (EPI) {
+            cx<float> xv[4][3];
+            Sio<FMT>::load(a.x, a.cs, i, xv);
+#pragma unroll
+            for (int s = 0; s < 4; s++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    acc[s][c].r = fmaf(a.coef, acc[s][c].r, xv[s][c].r);
+                    acc[s][c].i = fmaf(a.coef, acc[s][c].i, xv[s][c].i);
+                    nrm = fmaf(acc[s][c].r, acc[s][c].r, nrm);
+                    nrm = fmaf(acc[s][c].i, acc[s][c].i, nrm);
+                }
+        }
+        Sio<FMT>::store(a.res, a.cs, i, acc);
+    }
+    if constexpr (EPI) {
+        if (a.partials) block_sum_to<float>(a.partials, nrm);
+    }
+}
+
+}  // namespace gbds

@@ -1,0 +1,21 @@
+// Generalised Dslash, 16-bit spinor storage: bfloat16, and half with a
+// per-spinor norm.
+#include "dslash_gen_impl.cuh"
+
+namespace gbds {
+cudaError_t launch_gen_half(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,
+                            int isign, int cb, const void *x, float coef, double *partials, cudaStream_t st) {
+    if (fmt == kFmtBF16) return launch_gen_t<kFmtBF16>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st);
+    return launch_gen_t<kFmtF16N>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st);
+}
+cudaError_t launch_pack_gen_half(int fmt, const Geom &g, int nrhs, const float *packed, const int *table, int parity,
+                                 void *out, cudaStream_t st) {
+    if (fmt == kFmtBF16) return launch_pack_gen_t<kFmtBF16>(g, nrhs, packed, table, parity, out, st);
+    return launch_pack_gen_t<kFmtF16N>(g, nrhs, packed, table, parity, out, st);
+}
+cudaError_t launch_unpack_gen_half(int fmt, const Geom &g, int nrhs, const void *in, const int *table, int parity,
+                                   float *packed, cudaStream_t st) {
+    if (fmt == kFmtBF16) return launch_unpack_gen_t<kFmtBF16>(g, nrhs, in, table, parity, packed, st);
+    return launch_unpack_gen_t<kFmtF16N>(g, nrhs, in, table, parity, packed, st);
+}
+}  // namespace gbds

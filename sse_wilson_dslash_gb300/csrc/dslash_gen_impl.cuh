@@ -1,0 +1,105 @@
+// Launchers and layout kernels of the generalised Dslash (dslash_gen.cuh),
+// instantiated per storage format by dslash_gen_f32.cu / dslash_gen_half.cu.
+#pragma once
+
+#include "dslash_gen.cuh"
+
+namespace gbds {
+
+// packed: FP32 [nrhs][V][4][3][2] in caller order; thread per (h, r).
+template <int FMT>
+__global__ void pack_gen_kernel(const float *__restrict__ packed, const int *__restrict__ table, int parity, Geom g,
+                                int nrhs, size_t cs, char *out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.Vh * nrhs) return;
+    const int h = (int)(t / nrhs), r = (int)(t % nrhs);
+    const int i = parity * g.Vh + h;
+    const int c = table ? __ldg(table + i) : i;
+    const float *src = packed + ((size_t)r * g.V + c) * 24;
+    cx<float> s[4][3];
+#pragma unroll
+    for (int j = 0; j < 12; j++) s[j / 3][j % 3] = {src[2 * j], src[2 * j + 1]};
+    Sio<FMT>::store(out, cs, (size_t)h * nrhs + r, s);
+}
+
+template <int FMT>
+__global__ void unpack_gen_kernel(const char *in, const int *__restrict__ table, int parity, Geom g, int nrhs, size_t cs,
+                                  float *packed) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.Vh * nrhs) return;
+    const int h = (int)(t / nrhs), r = (int)(t % nrhs);
+    const int i = parity * g.Vh + h;
+    const int c = table ? __ldg(table + i) : i;
+    cx<float> s[4][3];
+    Sio<FMT>::load(in, cs, (size_t)h * nrhs + r, s);
+    float *dst = packed + ((size_t)r * g.V + c) * 24;
+#pragma unroll
+    for (int j = 0; j < 12; j++) {
+        dst[2 * j] = s[j / 3][j % 3].r;
+        dst[2 * j + 1] = s[j / 3][j % 3].i;
+    }
+}
+
+template <int FMT, int RECON, int ISIGN, int EPI>
+void launch_gen_nrhs(const GenArgs &a, int nrhs, dim3 grid, cudaStream_t st) {
+    switch (nrhs) {
+    case 1: dslash_gen_kernel<FMT, RECON, ISIGN, 1, EPI><<<grid, 128, 0, st>>>(a); break;
+    case 2: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 2, 0><<<grid, 128, 0, st>>>(a); break;
+    case 4: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 4, 0><<<grid, 128, 0, st>>>(a); break;
+    case 8: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 8, 0><<<grid, 128, 0, st>>>(a); break;
+    case 16: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 16, 0><<<grid, 128, 0, st>>>(a); break;
+    default: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 32, 0><<<grid, 128, 0, st>>>(a); break;
+    }
+}
+
+template <int FMT>
+cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
+                         int cb, const void *x, float coef, double *partials, cudaStream_t st) {
+    GenArgs a;
+    a.g = g;
+    a.psi = static_cast<const char *>(psi);
+    a.res = static_cast<char *>(res);
+    a.gauge = static_cast<const char *>(gauge);
+    a.link_block_bytes = (size_t)recon * 4 * g.stride;
+    a.cs = (size_t)g.stride * nrhs;
+    a.pt = 1 - cb;
+    a.x = static_cast<const char *>(x);
+    a.coef = coef;
+    a.partials = partials;
+    const long long n = (long long)g.Vh * nrhs;
+    const dim3 grid((unsigned)((n + 127) / 128));
+    const bool epi = x != nullptr;
+    if (epi && nrhs != 1) return cudaErrorInvalidValue;
+#define GBDS_GEN(R, S)                                                   \
+    do {                                                                 \
+        if (epi) launch_gen_nrhs<FMT, R, S, 1>(a, nrhs, grid, st);       \
+        else launch_gen_nrhs<FMT, R, S, 0>(a, nrhs, grid, st);           \
+    } while (0)
+    if (recon == 18) { if (isign > 0) GBDS_GEN(18, 1); else GBDS_GEN(18, -1); }
+    else             { if (isign > 0) GBDS_GEN(12, 1); else GBDS_GEN(12, -1); }
+#undef GBDS_GEN
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int FMT>
+cudaError_t launch_pack_gen_t(const Geom &g, int nrhs, const float *packed, const int *table, int parity, void *out,
+                              cudaStream_t st) {
+    const long long n = (long long)g.Vh * nrhs;
+    pack_gen_kernel<FMT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(packed, table, parity, g, nrhs,
+                                                                      (size_t)g.stride * nrhs, static_cast<char *>(out));
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int FMT>
+cudaError_t launch_unpack_gen_t(const Geom &g, int nrhs, const void *in, const int *table, int parity, float *packed,
+                                cudaStream_t st) {
+    const long long n = (long long)g.Vh * nrhs;
+    unpack_gen_kernel<FMT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(static_cast<const char *>(in), table, parity, g,
+                                                                        nrhs, (size_t)g.stride * nrhs, packed);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace gbds

@@ -52,6 +52,25 @@ cudaError_t launch_unpack_spinor(const Geom &g, int prec, const void *spinor, co
 cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_packed,
                               const int *site_table, void *gauge, cudaStream_t stream);
 
+// Generalised Dslash (dslash_gen_*.cu): FP32 arithmetic and links, nrhs in
+// {1,2,4,8,16,32}, spinor formats 0 FP32, 1 BF16, 2 FP16 + norm.  x != nullptr
+// selects the xpay epilogue res = x + coef * D psi (nrhs 1 only) with |res|^2
+// partials per 128-thread block.
+cudaError_t launch_gen_f32(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
+                           int cb, const void *x, float coef, double *partials, cudaStream_t st);
+cudaError_t launch_gen_half(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,
+                            int isign, int cb, const void *x, float coef, double *partials, cudaStream_t st);
+// packed: FP32 [nrhs][V][4][3][2], caller order
+cudaError_t launch_pack_gen_f32(const Geom &g, int nrhs, const float *packed, const int *table, int parity, void *out,
+                                cudaStream_t st);
+cudaError_t launch_unpack_gen_f32(const Geom &g, int nrhs, const void *in, const int *table, int parity, float *packed,
+                                  cudaStream_t st);
+cudaError_t launch_pack_gen_half(int fmt, const Geom &g, int nrhs, const float *packed, const int *table, int parity,
+                                 void *out, cudaStream_t st);
+cudaError_t launch_unpack_gen_half(int fmt, const Geom &g, int nrhs, const void *in, const int *table, int parity,
+                                   float *packed, cudaStream_t st);
+inline int gen_spinor_bytes(int fmt) { return fmt == 0 ? 96 : (fmt == 1 ? 48 : 52); }
+
 // Sizes in bytes of the internal fields.
 size_t spinor_bytes(const Geom &g, int prec);
 size_t gauge_bytes(const Geom &g, int prec, int recon);
@@ -67,5 +86,7 @@ struct gbds_op_s {
     int recon;
     int block;
     int variant;
+    int nrhs;    // right-hand sides per site (1 = the plain operator)
+    int format;  // spinor storage: 0 native (prec), 1 bfloat16, 2 half + per-spinor norm
     int *d_site_table;  // device copy of the layout table, or nullptr (canonical)
 };

@@ -428,6 +428,7 @@ extern "C" int gbds_solver_solve(gbds_solver s, const double *b_packed, double *
     const double c2 = s->hsc->outer_rr;
     double outer_rr = c2;
     int total = 0;
+    bool have_residual = false;  // r64 = c - A x and Mp64 = M x are current
     if (c2 > 0) {
         if (s->prm.inner_prec == 64) {
             // all-FP64 CG: r = p = c
@@ -476,6 +477,7 @@ extern "C" int gbds_solver_solve(gbds_solver s, const double *b_packed, double *
                 if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
                 if (e == cudaSuccess) e = read_scalars(s, st);
                 if (e != cudaSuccess) break;
+                have_residual = true;
                 const double prev = outer_rr;
                 outer_rr = s->hsc->outer_rr;
                 if (!(outer_rr < prev)) break;  // no progress (or NaN): stop
@@ -483,19 +485,25 @@ extern "C" int gbds_solver_solve(gbds_solver s, const double *b_packed, double *
         }
     }
     if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");
-    // FP64 checks: |c - A x| / |c| and |b - M x| / |b|
-    e = apply_M<double>(s, s->gauge64, 18, s->x64, s->t64, s->Mp64, +1, nullptr, st);
-    if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->Mp64, s->t64, s->Ap64, -1, nullptr, st);
+    // FP64 checks: |c - A x| / |c| and |b - M x| / |b|.  The defect-correction
+    // loop leaves both r = c - A x (norm in outer_rr) and M x (in Mp64) from
+    // its last cycle; the FP64 CG's recursive residual is not the true one, so
+    // there they are computed here.
     const int nb = blocks(g);
-    if (e == cudaSuccess) {
-        xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->c64), static_cast<const double2 *>(s->Ap64),
-                                          static_cast<double2 *>(s->r64), g.Vh, g.stride, s->partials);
-        count_launch();
-        e = cudaGetLastError();
+    double final_rr = outer_rr;
+    if (!have_residual) {
+        e = apply_M<double>(s, s->gauge64, 18, s->x64, s->t64, s->Mp64, +1, nullptr, st);
+        if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->Mp64, s->t64, s->Ap64, -1, nullptr, st);
+        if (e == cudaSuccess) {
+            xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->c64), static_cast<const double2 *>(s->Ap64),
+                                              static_cast<double2 *>(s->r64), g.Vh, g.stride, s->partials);
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
+        if (e == cudaSuccess) e = read_scalars(s, st);
+        final_rr = s->hsc->outer_rr;
     }
-    if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
-    if (e == cudaSuccess) e = read_scalars(s, st);
-    const double final_rr = s->hsc->outer_rr;
     if (e == cudaSuccess) {
         xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->b64), static_cast<const double2 *>(s->Mp64),
                                           static_cast<double2 *>(s->p64), g.Vh, g.stride, s->partials);

@@ -35,15 +35,19 @@ class DslashOperator:
     prec: 32 or 64; recon: 18 or 12 (12-real links, SU(3) only).
     """
 
-    def __init__(self, dims, nd: int = 4, prec: int = 32, recon: int = 18, device=None):
+    FORMATS = {"native": 0, "bf16": 1, "f16": 2}
+
+    def __init__(self, dims, nd: int = 4, prec: int = 32, recon: int = 18, device=None, nrhs: int = 1,
+                 spinor_format: str = "native"):
         import torch
         self.dims = tuple(int(v) for v in dims)
-        self.nd, self.prec, self.recon = nd, prec, recon
+        self.nd, self.prec, self.recon, self.nrhs = nd, prec, recon, nrhs
+        self.spinor_format = spinor_format
         self.device = torch.device("cuda" if device is None else device)
         L = _lib.core()
         h = ctypes.c_void_p()
         d = (ctypes.c_int * 4)(*self.dims)
-        _lib.check(L.gbds_op_create(ctypes.byref(h), d, nd, prec, recon))
+        _lib.check(L.gbds_op_create_ex(ctypes.byref(h), d, nd, prec, recon, nrhs, self.FORMATS[spinor_format]))
         self._h = h
         V, Vh, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _lib.check(L.gbds_op_geometry(h, ctypes.byref(V), ctypes.byref(Vh), ctypes.byref(st)))
@@ -51,6 +55,7 @@ class DslashOperator:
         self.spinor_bytes = int(L.gbds_op_spinor_bytes(h))
         self.gauge_bytes = int(L.gbds_op_gauge_bytes(h))
         self.real_dtype = torch.float32 if prec == 32 else torch.float64
+        # packed dtype of the gauge field (FP32 for the generalised formats)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -113,16 +118,16 @@ class DslashOperator:
         return out
 
     def pack_spinor(self, psi_packed, parity: int, out=None, stream=None):
-        """Packed device spinor ``[V][4][3][2]`` (checkerboard ``parity``) -> internal."""
+        """Packed device spinor ``[nrhs][V][4][3][2]`` (checkerboard ``parity``) -> internal."""
         out = self.new_spinor() if out is None else out
-        self._check_real(psi_packed, self.volume * 24)
+        self._check_real(psi_packed, self.volume * 24 * self.nrhs)
         _lib.check(_lib.core().gbds_op_pack_spinor(self._h, ctypes.c_void_p(_dptr(psi_packed)), int(parity),
                                                    ctypes.c_void_p(_dptr(out)), _stream(stream)))
         return out
 
     def unpack_spinor(self, spinor, parity: int, psi_packed, stream=None):
         """Internal spinor -> the checkerboard ``parity`` sites of a packed array."""
-        self._check_real(psi_packed, self.volume * 24)
+        self._check_real(psi_packed, self.volume * 24 * self.nrhs)
         _lib.check(_lib.core().gbds_op_unpack_spinor(self._h, ctypes.c_void_p(_dptr(spinor)), int(parity),
                                                      ctypes.c_void_p(_dptr(psi_packed)), _stream(stream)))
         return psi_packed
@@ -151,9 +156,11 @@ class DslashOperator:
 
     @property
     def bytes_per_site(self) -> int:
-        """Compulsory HBM bytes per output site: 2 spinors + 2*nd links."""
+        """Compulsory HBM bytes per output site and right-hand side: 2 spinors +
+        2*nd links shared by the nrhs right-hand sides."""
         real = 4 if self.prec == 32 else 8
-        return 2 * 24 * real + 2 * self.nd * self.recon * real
+        spinor = {"native": 24 * real, "bf16": 48, "f16": 52}[self.spinor_format]
+        return 2 * spinor + 2 * self.nd * self.recon * real / self.nrhs
 
 
 class WilsonSolver:

@@ -1,0 +1,65 @@
+"""Several right-hand sides per site and 16-bit spinor storage (GPU), each
+right-hand side checked against the oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+# Per-site tolerances: FP32 as the parity tests; bfloat16 storage rounds
+# inputs and outputs to 8 significant bits (2^-9 relative per component);
+# half + norm to 11 bits of the site's largest component.
+TOL = {"native": 1e-6, "bf16": 1.2e-2, "f16": 3e-3}
+
+
+def _round(psi, fmt):
+    import torch
+    t = torch.from_numpy(psi.astype(np.float32))
+    if fmt == "bf16":
+        return t.to(torch.bfloat16).float().numpy().astype(np.float64)
+    if fmt == "f16":
+        v = t.reshape(-1, 24)
+        m = v.abs().amax(1, keepdim=True)
+        q = (v / torch.where(m > 0, m, torch.ones_like(m))).half().float() * m
+        return q.reshape(t.shape).numpy().astype(np.float64)
+    return psi.astype(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("fmt", ["native", "bf16", "f16"])
+@pytest.mark.parametrize("nrhs", [1, 2, 4, 8, 16, 32])
+def test_multi_rhs_matches_oracle(nrhs, fmt):
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    if fmt != "native" and nrhs in (2, 16):
+        pytest.skip("covered by the other counts")
+    dims = (8, 4, 6, 4)
+    V = O.volume(dims)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    rng = np.random.default_rng(nrhs)
+    u = O.random_gauge(rng, V)
+    psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
+    for recon in (18, 12):
+        op = DslashOperator(dims, nd=4, prec=32, recon=recon, nrhs=nrhs, spinor_format=fmt)
+        gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
+        packed = torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda()
+        for isign, cb in ((1, 0), (-1, 1)):
+            src = op.pack_spinor(packed, cb)
+            out = op.apply(gauge, src, isign, cb)
+            res = torch.zeros(nrhs * V * 24, dtype=torch.float32, device="cuda")
+            op.unpack_spinor(out, 1 - cb, res)
+            got = res.cpu().numpy().reshape(nrhs, V, 24)
+            ts = O.target_sites(4, dims, lol, cb)
+            for r in range(nrhs):
+                ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
+                err = O.site_rel_err(got[r], ref, ts)
+                assert err <= TOL[fmt], (recon, isign, cb, r, err)
+        op.close()
+
+
+def test_multi_rhs_bytes_accounting():
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    op = DslashOperator((4, 4, 4, 4), nrhs=16, spinor_format="bf16", recon=12)
+    assert op.bytes_per_site == 2 * 48 + 8 * 48 / 16
+    assert op.spinor_bytes == 48 * op.stride * 16
+    op.close()
