@@ -183,6 +183,24 @@ int gbds_dslash_packed_noalloc_f32(const int dims[4], int nd, const float *u_pac
                                    float *res_packed, int isign, int cb, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Adjoint and force                                                         */
+/* ------------------------------------------------------------------------ */
+/* For L = Re <chi, Dslash(isign) psi> (psi: internal field on checkerboard
+ * cb, chi: on 1-cb; no counterpart in the reference):
+ *   dL/dpsi = Dslash(-isign) chi  -- gbds_op_dslash with -isign, source 1-cb;
+ *   dL/dU   -- this call, for every link of the lattice (forward hops own the
+ *              links on checkerboard 1-cb, backward hops those on cb):
+ *     mode 0: G = dL/dRe U + i dL/dIm U, the complex gradient;
+ *     mode 1: F = TA(G U^+), the traceless anti-Hermitian (su(3)) force, so
+ *             that along U -> exp(eps X) U, dL/deps = Re tr(F^+ X).
+ * Written to force_packed, FP32/FP64 as the operator, in the packed gauge
+ * layout [V][4][3][3][2] with f[s][mu][j][i] = R_ij (R = G or F), caller
+ * order; accumulate = 1 adds coef * R to it, 0 stores coef * R.
+ * Needs a 4D, single right-hand side, native-format, recon 18 operator. */
+int gbds_op_force(gbds_op op, const void *gauge, const void *psi, const void *chi, int isign, int cb, int mode,
+                  double coef, int accumulate, void *force_packed, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Even-odd preconditioned Wilson solver                                     */
 /* ------------------------------------------------------------------------ */
 /* M = 1 - kappa^2 D_eo D_oe on checkerboard 0 (even sites), D the operator
@@ -224,6 +242,10 @@ int gbds_solver_apply(gbds_solver s, const double *x_packed, double *y_packed, i
  * written on the even sites only; it starts from zero). */
 int gbds_solver_solve(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats,
                       void *stream);
+/* Solve the normal equations M^+ M x = c directly (c given on the even sites;
+ * stats->true_residual then reports |c - M^+ M x| / |c|). */
+int gbds_solver_solve_normal(gbds_solver s, const double *c_packed, double *x_packed, gbds_solver_stats *stats,
+                             void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Reference entry points with precision suffixes                            */

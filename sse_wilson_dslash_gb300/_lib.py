@@ -86,6 +86,8 @@ def core() -> ctypes.CDLL:
     L.gbds_solver_set_gauge.argtypes = [vp, vp, vp]
     L.gbds_solver_apply.argtypes = [vp, vp, vp, i, vp]
     L.gbds_solver_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
+    L.gbds_solver_solve_normal.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
+    L.gbds_op_force.argtypes = [vp, vp, vp, vp, i, i, i, ctypes.c_double, i, vp, vp]
     _core = L
     return L
 

@@ -406,8 +406,21 @@ extern "C" int gbds_solver_apply(gbds_solver s, const double *x_packed, double *
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "gbds_solver_apply");
 }
 
+static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats, void *stream,
+                      bool normal);
+
 extern "C" int gbds_solver_solve(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats,
                                  void *stream) {
+    return solve_impl(s, b_packed, x_packed, stats, stream, false);
+}
+
+extern "C" int gbds_solver_solve_normal(gbds_solver s, const double *c_packed, double *x_packed, gbds_solver_stats *stats,
+                                        void *stream) {
+    return solve_impl(s, c_packed, x_packed, stats, stream, true);
+}
+
+static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats, void *stream,
+                      bool normal) {
     if (!s) return set_error(GBDS_ERROR_NOT_INITIALIZED, "solver is NULL");
     if (!s->have_gauge) return set_error(GBDS_ERROR_NOT_INITIALIZED, "gbds_solver_set_gauge has not been called");
     if (!b_packed || !x_packed) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL field pointer");
@@ -419,9 +432,12 @@ extern "C" int gbds_solver_solve(gbds_solver s, const double *b_packed, double *
     const Geom &g = s->g;
     const double tol2 = s->prm.tol * s->prm.tol;
     // b, c = M^+ b, |c|^2
-    cudaError_t e = launch_pack_spinor(g, 64, b_packed, nullptr, 0, 0, s->b64, st);
-    if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->b64, s->t64, s->c64, -1, s->partials, st);
-    if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
+    cudaError_t e = launch_pack_spinor(g, 64, b_packed, nullptr, 0, 0, normal ? s->c64 : s->b64, st);
+    if (e == cudaSuccess) {
+        if (normal) e = norm_into<double>(s, s->c64, nullptr, nullptr, kOuterRR, st);
+        else e = apply_M<double>(s, s->gauge64, 18, s->b64, s->t64, s->c64, -1, s->partials, st);
+    }
+    if (e == cudaSuccess && !normal) e = finish_on(s, kOuterRR, st);
     if (e == cudaSuccess) e = zero<double>(s, s->x64, st);
     if (e == cudaSuccess) e = read_scalars(s, st);
     if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");
@@ -504,15 +520,20 @@ extern "C" int gbds_solver_solve(gbds_solver s, const double *b_packed, double *
         if (e == cudaSuccess) e = read_scalars(s, st);
         final_rr = s->hsc->outer_rr;
     }
-    if (e == cudaSuccess) {
-        xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->b64), static_cast<const double2 *>(s->Mp64),
-                                          static_cast<double2 *>(s->p64), g.Vh, g.stride, s->partials);
-        count_launch();
-        e = cudaGetLastError();
+    if (!normal) {
+        if (e == cudaSuccess) {
+            xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->b64), static_cast<const double2 *>(s->Mp64),
+                                              static_cast<double2 *>(s->p64), g.Vh, g.stride, s->partials);
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = finish_on(s, kNorm, st);
+        if (e == cudaSuccess) e = norm_into<double>(s, s->b64, nullptr, nullptr, kOuterRR, st);
+        if (e == cudaSuccess) e = read_scalars(s, st);
+    } else {
+        s->hsc->norm = final_rr;
+        s->hsc->outer_rr = c2;
     }
-    if (e == cudaSuccess) e = finish_on(s, kNorm, st);
-    if (e == cudaSuccess) e = norm_into<double>(s, s->b64, nullptr, nullptr, kOuterRR, st);
-    if (e == cudaSuccess) e = read_scalars(s, st);
     if (e == cudaSuccess) e = launch_unpack_spinor(g, 64, s->x64, nullptr, 0, 0, x_packed, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");

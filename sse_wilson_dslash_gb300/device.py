@@ -142,6 +142,17 @@ class DslashOperator:
                                               ctypes.c_void_p(_dptr(out)), int(isign), int(cb), _stream(stream)))
         return out
 
+    def force(self, gauge, psi, chi, isign: int, cb: int, out, mode: int = 1, coef: float = 1.0,
+              accumulate: bool = False, stream=None):
+        """dL/dU for L = Re <chi, Dslash(isign) psi> (psi on cb, chi on 1-cb,
+        internal fields) into the packed gauge-layout tensor ``out``: mode 0
+        the complex gradient G, mode 1 the su(3) force TA(G U^+)."""
+        self._check_real(out, self.volume * 72)
+        _lib.check(_lib.core().gbds_op_force(self._h, ctypes.c_void_p(_dptr(gauge)), ctypes.c_void_p(_dptr(psi)),
+                                             ctypes.c_void_p(_dptr(chi)), int(isign), int(cb), int(mode), float(coef),
+                                             1 if accumulate else 0, ctypes.c_void_p(_dptr(out)), _stream(stream)))
+        return out
+
     def _check_real(self, t, n):
         if t.dtype != self.real_dtype:
             raise TypeError(f"expected {self.real_dtype}")
@@ -209,10 +220,11 @@ class WilsonSolver:
                                                  1 if dagger else 0, _stream(stream)))
         return y
 
-    def solve(self, b, x, stream=None) -> dict:
+    def solve(self, b, x, stream=None, normal: bool = False) -> dict:
+        """M x = b, or with normal=True M^+ M x = b (b then the normal-equation right-hand side)."""
         self._check(b, self.volume * 24)
         self._check(x, self.volume * 24)
         st = _lib.SolverStats()
-        _lib.check(_lib.core().gbds_solver_solve(self._h, ctypes.c_void_p(_dptr(b)), ctypes.c_void_p(_dptr(x)),
-                                                 ctypes.byref(st), _stream(stream)))
+        f = _lib.core().gbds_solver_solve_normal if normal else _lib.core().gbds_solver_solve
+        _lib.check(f(self._h, ctypes.c_void_p(_dptr(b)), ctypes.c_void_p(_dptr(x)), ctypes.byref(st), _stream(stream)))
         return {k: getattr(st, k) for k, _ in st._fields_}
