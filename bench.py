@@ -287,6 +287,7 @@ def profiled_traffic(workload):
         return None
     for ln in open(p):
         if ln.strip().startswith("traffic_bytes_per_launch:"):
+            # measured for one launch by ncu (dram__bytes_read.sum + dram__bytes_write.sum)
             try:
                 return int(float(ln.split(":", 1)[1].strip()))
             except ValueError:
