@@ -271,6 +271,62 @@ def multi_rhs_variants(torch, steps, peak):
     return out
 
 
+def uneven_batch(torch, peak):
+    """16^4 (8 rhs), 20^3x40 (4), 24^3x48 (2), 32^3x64 (1), each with its own
+    random SU(3) gauge field: four separate launches vs one persistent launch
+    (autotuned schedule) vs the same launch replayed from a CUDA graph."""
+    from sse_wilson_dslash_gb300.device import DslashBatch, DslashOperator
+    specs = [((16, 16, 16, 16), 8), ((20, 20, 20, 40), 4), ((24, 24, 24, 48), 2), ((32, 32, 32, 64), 1)]
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    items = []
+    for dims, nrhs in specs:
+        op = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs)
+        V = op.volume
+        u = su3_links(V * 4, gen, torch).float().reshape(-1)
+        gauge = op.pack_gauge(u)
+        del u
+        psi = torch.randn(nrhs * V * 24, dtype=torch.float32, device="cuda", generator=gen)
+        items.append(dict(op=op, gauge=gauge, psi=op.pack_spinor(psi, 0), res=op.new_spinor(), isign=1, cb=0))
+        del psi
+    work = sum(1320 * it["op"].volume_cb * it["op"].nrhs for it in items)
+    nbytes = sum(it["op"].bytes_per_site * it["op"].volume_cb * it["op"].nrhs for it in items)
+    stream = torch.cuda.Stream()
+    reps = 50
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def separate():
+        for it in items:
+            it["op"].apply(it["gauge"], it["psi"], 1, 0, out=it["res"], stream=stream)
+
+    ms_sep = timed(separate)
+    b = DslashBatch(items)
+    with torch.cuda.stream(stream):
+        sched = b.autotune(stream)
+    ms_one = timed(lambda: b.launch(stream))
+    with torch.cuda.stream(stream):
+        b.capture_graph(stream)
+    ms_graph = timed(lambda: b.launch(stream))
+    b.close()
+    out = {"lattices": [dict(dims=list(d), nrhs=n) for d, n in specs], "schedule": sched,
+           "separate_ms": ms_sep, "one_launch_ms": ms_one, "graph_ms": ms_graph,
+           "gflops_graph": work / (ms_graph * 1e6), "gbs_graph": nbytes / (ms_graph * 1e6),
+           "roofline_frac_graph": nbytes / (ms_graph * 1e6) / peak}
+    for it in items:
+        it["op"].close()
+    return out
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -552,6 +608,8 @@ def run_gb300(args):
         for v in variants.values():
             v["roofline_frac"] = v["gbs"] / peak
         variants["multi_rhs_24x24x24x48"] = multi_rhs_variants(torch, vsteps, peak)
+        torch.cuda.empty_cache()
+        variants["uneven_batch"] = uneven_batch(torch, peak)
 
     solver = None
     if not args.no_solver:

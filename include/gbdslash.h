@@ -91,8 +91,8 @@ int gbds_op_destroy(gbds_op op);
 #define GBDS_SPINOR_BF16 1     /* 24 bfloat16 per spinor (48 B)                */
 #define GBDS_SPINOR_F16_NORM 2 /* 24 half scaled by a per-spinor float norm (52 B) */
 
-/* As gbds_op_create, for nrhs right-hand sides per site (1, 2, 4, 8, 16 or
- * 32) and a spinor storage format.  nrhs > 1 or a 16-bit format needs
+/* As gbds_op_create, for nrhs right-hand sides per site (1..32; powers of two
+ * have specialised kernels) and a spinor storage format.  nrhs > 1 or a 16-bit format needs
  * prec 32 and nd 4; arithmetic is FP32.  A field then holds nrhs spinors per
  * site, element (k, h, r) at k*stride*nrhs + h*nrhs + r (k: 16-byte component,
  * h: site, r: right-hand side), half formats followed by one float norm per
@@ -181,6 +181,44 @@ long long gbds_kernel_launch_count(void);
 #define GBDS_NOALLOC_SCRATCH_BYTES 12582912
 int gbds_dslash_packed_noalloc_f32(const int dims[4], int nd, const float *u_packed, const float *psi_packed,
                                    float *res_packed, int isign, int cb, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Uneven batches                                                            */
+/* ------------------------------------------------------------------------ */
+/* Several lattices -- each with its own size, FP32 gauge field, spinors,
+ * number of right-hand sides, isign and cb -- applied by one persistent
+ * kernel launch (no counterpart in the reference).  Fields are the internal
+ * ones of gbds_op_create_ex(dims, 4, 32, recon, nrhs, format) for the item's
+ * dims and nrhs (gauge from gbds_op_pack_gauge, spinors from
+ * gbds_op_pack_spinor); recon and format are common to the batch.  The work
+ * list (tiles of (site, rhs) pairs) is built at create time; each CTA of the
+ * launch walks it with a fixed stride, so no CTA waits on another and the
+ * launch can be captured in a CUDA graph (gbds_batch_capture_graph; later
+ * gbds_batch_launch calls replay the graph).  Pointers are fixed at create
+ * time. */
+typedef struct gbds_batch_item {
+    int dims[4];
+    int nrhs;
+    int isign;
+    int cb;
+    const void *gauge;
+    const void *psi;
+    void *res;
+} gbds_batch_item;
+
+typedef struct gbds_batch_s *gbds_batch;
+
+int gbds_batch_create(gbds_batch *b, const gbds_batch_item *items, int n, int recon, int format);
+int gbds_batch_destroy(gbds_batch b);
+/* Schedule: threads per tile (multiple of 32, <= 256), resident CTAs (0 =
+ * one per tile), order 0 (lattice after lattice) or 1 (interleaved). */
+int gbds_batch_set_schedule(gbds_batch b, int tile_threads, int resident_ctas, int order);
+int gbds_batch_get_schedule(gbds_batch b, int *tile_threads, int *resident_ctas, int *order, int *ntiles);
+/* Time the candidate schedules on the batch's own fields (res is overwritten)
+ * and keep the fastest.  Drops a captured graph. */
+int gbds_batch_autotune(gbds_batch b, void *stream);
+int gbds_batch_capture_graph(gbds_batch b, void *stream);
+int gbds_batch_launch(gbds_batch b, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Adjoint and force                                                         */

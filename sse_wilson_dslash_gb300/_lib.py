@@ -32,6 +32,12 @@ class SolverStats(ctypes.Structure):
                 ("residual", ctypes.c_double), ("true_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
 
 
+class BatchItem(ctypes.Structure):
+    """gbds_batch_item (include/gbdslash.h)."""
+    _fields_ = [("dims", ctypes.c_int * 4), ("nrhs", ctypes.c_int), ("isign", ctypes.c_int), ("cb", ctypes.c_int),
+                ("gauge", ctypes.c_void_p), ("psi", ctypes.c_void_p), ("res", ctypes.c_void_p)]
+
+
 class GbdsError(RuntimeError):
     """A gbds_* call returned a non-zero status."""
 
@@ -88,6 +94,13 @@ def core() -> ctypes.CDLL:
     L.gbds_solver_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
     L.gbds_solver_solve_normal.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
     L.gbds_op_force.argtypes = [vp, vp, vp, vp, i, i, i, ctypes.c_double, i, vp, vp]
+    L.gbds_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(BatchItem), i, i, i]
+    L.gbds_batch_destroy.argtypes = [vp]
+    L.gbds_batch_set_schedule.argtypes = [vp, i, i, i]
+    L.gbds_batch_get_schedule.argtypes = [vp, c_int_p, c_int_p, c_int_p, c_int_p]
+    L.gbds_batch_autotune.argtypes = [vp, vp]
+    L.gbds_batch_capture_graph.argtypes = [vp, vp]
+    L.gbds_batch_launch.argtypes = [vp, vp]
     _core = L
     return L
 

@@ -98,8 +98,7 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     *op = nullptr;
     if (prec != 32 && prec != 64) return set_error(GBDS_ERROR_INVALID_VALUE, "prec must be 32 or 64");
     if (recon != 18 && recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "recon must be 18 or 12");
-    if (nrhs != 1 && nrhs != 2 && nrhs != 4 && nrhs != 8 && nrhs != 16 && nrhs != 32)
-        return set_error(GBDS_ERROR_INVALID_VALUE, "nrhs must be 1, 2, 4, 8, 16 or 32");
+    if (nrhs < 1 || nrhs > 32) return set_error(GBDS_ERROR_INVALID_VALUE, "nrhs must be in [1, 32]");
     if (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_BF16 && format != GBDS_SPINOR_F16_NORM)
         return set_error(GBDS_ERROR_INVALID_VALUE, "unknown spinor format");
     if ((nrhs > 1 || format != GBDS_SPINOR_NATIVE) && (prec != 32 || nd != 4))

@@ -138,6 +138,7 @@ struct GenArgs {
     const char *gauge;         // FP32 links, both checkerboards
     size_t link_block_bytes;   // one (parity, mu) block
     size_t cs;                 // component stride of the spinor arrays (elements) = stride * NRHS
+    int nrhs;                  // right-hand sides (used when the kernel's NRHS is 0)
     int pt;                    // target parity
     // xpay epilogue: res = x + coef * D psi, |res|^2 partials
     const char *x;
@@ -145,16 +146,21 @@ struct GenArgs {
     double *partials;
 };
 
+// NRHS > 0: compile-time count; NRHS == 0: a.nrhs at run time.
+template <int NRHS>
+__device__ __forceinline__ int nrhs_of(const GenArgs &a) { return NRHS > 0 ? NRHS : a.nrhs; }
+
 template <int FMT, int RECON, int ISIGN, int NRHS, int MU>
 __device__ __forceinline__ void gen_hop_pair(const GenArgs &a, int h, int r, const Nbr &n, cx<float> (&acc)[4][3]) {
     const int ps = 1 - a.pt;
+    const int nr = nrhs_of<NRHS>(a);
     cx<float> s[4][3], hs[2][3], w[2][3], U[3][3];
-    Sio<FMT>::load(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, s);
+    Sio<FMT>::load(a.psi, a.cs, (size_t)n.f[MU] * nr + r, s);
     Field<float>::template load_link<RECON>(a.gauge + (size_t)(a.pt * 4 + MU) * a.link_block_bytes, a.g.stride, h, U);
     project<MU, ISIGN>(s, hs);
     su3_mul<false>(U, hs, w);
     reconstruct<MU, ISIGN>(acc, w);
-    Sio<FMT>::load(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, s);
+    Sio<FMT>::load(a.psi, a.cs, (size_t)n.b[MU] * nr + r, s);
     Field<float>::template load_link<RECON>(a.gauge + (size_t)(ps * 4 + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
     project<MU, -ISIGN>(s, hs);
     su3_mul<true>(U, hs, w);
@@ -165,7 +171,8 @@ __device__ __forceinline__ void gen_hop_pair(const GenArgs &a, int h, int r, con
 template <int FMT, int RECON, int ISIGN, int NRHS, int EPI>
 __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int h = t / NRHS, r = t % NRHS;
+    const int nr = nrhs_of<NRHS>(a);
+    const int h = t / nr, r = t - h * nr;
     float nrm = 0.f;
     if (h < a.g.Vh) {
         Nbr n;
@@ -179,7 +186,7 @@ __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
         gen_hop_pair<FMT, RECON, ISIGN, NRHS, 1>(a, h, r, n, acc);
         gen_hop_pair<FMT, RECON, ISIGN, NRHS, 2>(a, h, r, n, acc);
         gen_hop_pair<FMT, RECON, ISIGN, NRHS, 3>(a, h, r, n, acc);
-        const size_t i = (size_t)h * NRHS + r;
+        const size_t i = (size_t)h * nr + r;
         if constexpr (EPI) {
             cx<float> xv[4][3];
             Sio<FMT>::load(a.x, a.cs, i, xv);

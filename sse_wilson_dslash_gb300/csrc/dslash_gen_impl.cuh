@@ -48,7 +48,8 @@ void launch_gen_nrhs(const GenArgs &a, int nrhs, dim3 grid, cudaStream_t st) {
     case 4: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 4, 0><<<grid, 128, 0, st>>>(a); break;
     case 8: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 8, 0><<<grid, 128, 0, st>>>(a); break;
     case 16: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 16, 0><<<grid, 128, 0, st>>>(a); break;
-    default: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 32, 0><<<grid, 128, 0, st>>>(a); break;
+    case 32: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 32, 0><<<grid, 128, 0, st>>>(a); break;
+    default: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 0, 0><<<grid, 128, 0, st>>>(a); break;
     }
 }
 
@@ -62,6 +63,7 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     a.gauge = static_cast<const char *>(gauge);
     a.link_block_bytes = (size_t)recon * 4 * g.stride;
     a.cs = (size_t)g.stride * nrhs;
+    a.nrhs = nrhs;
     a.pt = 1 - cb;
     a.x = static_cast<const char *>(x);
     a.coef = coef;

@@ -228,3 +228,56 @@ class WilsonSolver:
         f = _lib.core().gbds_solver_solve_normal if normal else _lib.core().gbds_solver_solve
         _lib.check(f(self._h, ctypes.c_void_p(_dptr(b)), ctypes.c_void_p(_dptr(x)), ctypes.byref(st), _stream(stream)))
         return {k: getattr(st, k) for k, _ in st._fields_}
+
+
+class DslashBatch:
+    """Several lattices applied by one persistent launch (gbds_batch_* in
+    include/gbdslash.h).  ``items``: list of dicts with keys op
+    (a DslashOperator of the item's dims/nrhs, prec 32, nd 4), gauge, psi, res
+    (internal fields of that op), isign, cb.  Fields must stay alive."""
+
+    def __init__(self, items, recon: int = 18, spinor_format: str = "native"):
+        arr = (_lib.BatchItem * len(items))()
+        for k, it in enumerate(items):
+            op = it["op"]
+            arr[k].dims = (ctypes.c_int * 4)(*op.dims)
+            arr[k].nrhs = op.nrhs
+            arr[k].isign = int(it["isign"])
+            arr[k].cb = int(it["cb"])
+            arr[k].gauge = _dptr(it["gauge"])
+            arr[k].psi = _dptr(it["psi"])
+            arr[k].res = _dptr(it["res"])
+        h = ctypes.c_void_p()
+        _lib.check(_lib.core().gbds_batch_create(ctypes.byref(h), arr, len(items), int(recon),
+                                                 DslashOperator.FORMATS[spinor_format]))
+        self._h = h
+        self._items = items
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.core().gbds_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def schedule(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        _lib.check(_lib.core().gbds_batch_get_schedule(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(tile_threads=v[0].value, resident_ctas=v[1].value, order=v[2].value, tiles=v[3].value)
+
+    def set_schedule(self, tile_threads: int, resident_ctas: int, order: int):
+        _lib.check(_lib.core().gbds_batch_set_schedule(self._h, tile_threads, resident_ctas, order))
+
+    def autotune(self, stream=None):
+        _lib.check(_lib.core().gbds_batch_autotune(self._h, _stream(stream)))
+        return self.schedule()
+
+    def capture_graph(self, stream):
+        _lib.check(_lib.core().gbds_batch_capture_graph(self._h, _stream(stream)))
+
+    def launch(self, stream=None):
+        _lib.check(_lib.core().gbds_batch_launch(self._h, _stream(stream)))
