@@ -22,6 +22,24 @@ def _item(dims, nrhs, isign, cb, recon, fmt, seed, torch):
     return dict(op=op, gauge=gauge, psi=src, res=op.new_spinor(), isign=isign, cb=cb, ref=ref)
 
 
+# The batch kernel and the per-operator kernel do the same arithmetic in the
+# same order, but the compiler may contract multiply-adds differently in the
+# two kernels: FP32 results agree to rounding, and a rounding difference can
+# move a 16-bit stored value by one unit.
+TOL = {"native": 1e-5, "bf16": 1e-2, "f16": 2e-3}
+
+
+def _same(op, a, b, fmt):
+    import torch
+    fa = torch.zeros(op.nrhs * op.volume * 24, dtype=torch.float32, device="cuda")
+    fb = torch.zeros_like(fa)
+    op.unpack_spinor(a, 0, fa)
+    op.unpack_spinor(a, 1, fa)
+    op.unpack_spinor(b, 0, fb)
+    op.unpack_spinor(b, 1, fb)
+    return float((fa - fb).abs().max()) <= TOL[fmt] * float(fb.abs().max())
+
+
 @pytest.mark.parametrize("recon,fmt", [(18, "native"), (12, "native"), (18, "bf16"), (12, "f16")])
 def test_batch_matches_single_operators(recon, fmt):
     import torch
@@ -35,7 +53,7 @@ def test_batch_matches_single_operators(recon, fmt):
     b.launch()
     torch.cuda.synchronize()
     for it in items:
-        assert torch.equal(it["res"], it["ref"])
+        assert _same(it["op"], it["res"], it["ref"], fmt)
     sch = b.autotune()
     assert sch["tile_threads"] in (64, 128, 256) and sch["tiles"] > 0
     for it in items:
@@ -47,7 +65,7 @@ def test_batch_matches_single_operators(recon, fmt):
             b.launch(s)
     s.synchronize()
     for it in items:
-        assert torch.equal(it["res"], it["ref"])
+        assert _same(it["op"], it["res"], it["ref"], fmt)
     b.close()
 
 
