@@ -222,11 +222,9 @@ def time_device(op, gauge, srcs, outs, steps, warmup, torch):
     return e0.elapsed_time(e1) / steps
 
 
-def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None, arith="ieee"):
+def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None):
     from sse_wilson_dslash_gb300.device import DslashOperator
     op = DslashOperator(dims, nd=nd, prec=prec, recon=recon)
-    if arith != "ieee":
-        op.set_arith(arith)
     dt = torch.float32 if prec == 32 else torch.float64
     u, psi = fields if fields is not None else make_fields(dims, dt, torch)
     gauge = op.pack_gauge(u)
@@ -603,10 +601,6 @@ def run_gb300(args):
         torch.cuda.empty_cache()
         variants["f64_recon18"] = device_variant(DIMS, 4, 64, 18, vsteps, 5, torch, fields=(u64, psi64))
         variants["f64_recon12"] = device_variant(DIMS, 4, 64, 12, vsteps, 5, torch, fields=(u64, psi64))
-        variants["f64_df64_recon18"] = device_variant(DIMS, 4, 64, 18, vsteps, 5, torch, fields=(u64, psi64),
-                                                      arith="df64")
-        variants["f64_df64_recon12"] = device_variant(DIMS, 4, 64, 12, vsteps, 5, torch, fields=(u64, psi64),
-                                                      arith="df64")
         del u64, psi64
         torch.cuda.empty_cache()
         variants["3d_24x24x24x48_f32_recon18"] = device_variant(DIMS_3D, 3, 32, 18, vsteps, 5, torch)

@@ -102,19 +102,6 @@ int gbds_op_destroy(gbds_op op);
 int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int prec, int recon, int nrhs, int format);
 int gbds_op_nrhs(gbds_op op);
 
-/* Arithmetic of a prec 64 operator:
- *   GBDS_ARITH_IEEE (default) IEEE FP64 fields and arithmetic;
- *   GBDS_ARITH_DF64 fields hold float-float pairs (hi + lo, ~48 significant
- *     bits, same 16 bytes per complex) and the Dslash runs in float-float
- *     arithmetic on the FP32 units (error-free TwoSum / FMA TwoProd), about
- *     1e-14 relative per site instead of 1e-16, several times faster on GPUs
- *     whose FP64 rate is low.  pack/unpack convert from / to IEEE doubles.
- * Set before packing fields. */
-#define GBDS_ARITH_IEEE 0
-#define GBDS_ARITH_DF64 1
-int gbds_op_set_arith(gbds_op op, int mode);
-int gbds_op_get_arith(gbds_op op);
-
 /* Caller site layout for pack/unpack: site_table[i] = caller linear index of
  * internal site i (i = p*Vh + h, internal order above), n = V entries, a
  * permutation of [0, V).  NULL (or the identity) selects the canonical
@@ -221,7 +208,6 @@ typedef struct gbds_batch_item {
 
 typedef struct gbds_batch_s *gbds_batch;
 
-/* n <= 32 lattices. */
 int gbds_batch_create(gbds_batch *b, const gbds_batch_item *items, int n, int recon, int format);
 int gbds_batch_destroy(gbds_batch b);
 /* Schedule: threads per tile (multiple of 32, <= 256), resident CTAs (0 =
@@ -380,10 +366,6 @@ int gbds_legacy_set_recon(int recon);
  *               otherwise as 1;
  * 1           - stage every array through cudaMemcpyAsync. */
 int gbds_legacy_set_host_access(int mode);
-/* Arithmetic of the FP64 legacy contexts (GBDS_ARITH_IEEE default, or
- * GBDS_ARITH_DF64); takes effect at the next init. */
-int gbds_legacy_set_fp64_arith(int mode);
-
 /* Path taken by the last legacy apply: 1 direct, 0 staged, -1 none yet. */
 int gbds_legacy_last_path(void);
 

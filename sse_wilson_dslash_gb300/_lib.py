@@ -66,8 +66,6 @@ def core() -> ctypes.CDLL:
     L.gbds_op_create.argtypes = [ctypes.POINTER(vp), c_int_p, i, i, i]
     L.gbds_op_create_ex.argtypes = [ctypes.POINTER(vp), c_int_p, i, i, i, i, i]
     L.gbds_op_nrhs.argtypes = [vp]
-    L.gbds_op_set_arith.argtypes = [vp, i]
-    L.gbds_op_get_arith.argtypes = [vp]
     L.gbds_op_destroy.argtypes = [vp]
     L.gbds_op_set_layout.argtypes = [vp, c_int_p, i]
     L.gbds_op_is_canonical.argtypes = [vp]
@@ -85,7 +83,7 @@ def core() -> ctypes.CDLL:
     L.gbds_op_unpack_spinor.argtypes = [vp, vp, i, vp, vp]
     L.gbds_op_dslash.argtypes = [vp, vp, vp, vp, i, i, vp]
     for n in ("gbds_legacy_set_exit_on_error", "gbds_legacy_set_gauge_cache", "gbds_legacy_set_recon",
-              "gbds_legacy_set_host_access", "gbds_legacy_set_fp64_arith"):
+              "gbds_legacy_set_host_access"):
         getattr(L, n).argtypes = [i]
     L.gbds_legacy_refcount.argtypes = [i, i]
     L.gbds_layout_select.argtypes = [i, c_int_p]

@@ -117,7 +117,6 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     // FP64 (FP64-issue bound) is insensitive.
     o->block = (prec == 32 && recon == 12) ? 64 : 128;
     o->variant = (prec == 32 && recon == 18) ? 1 : 0;
-    o->arith = 0;
     o->nrhs = nrhs;
     o->format = format;
     o->d_site_table = nullptr;
@@ -171,19 +170,6 @@ extern "C" size_t gbds_op_spinor_bytes(gbds_op op) {
 }
 
 extern "C" int gbds_op_nrhs(gbds_op op) { return op ? op->nrhs : 0; }
-
-static int df_of(gbds_op op) { return op->prec == 64 && op->arith == 1; }
-
-extern "C" int gbds_op_set_arith(gbds_op op, int mode) {
-    if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
-    if (mode != GBDS_ARITH_IEEE && mode != GBDS_ARITH_DF64) return set_error(GBDS_ERROR_INVALID_VALUE, "unknown arithmetic mode");
-    if (mode == GBDS_ARITH_DF64 && (op->prec != 64 || generic(op)))
-        return set_error(GBDS_ERROR_UNSUPPORTED, "float-float arithmetic is for prec 64 single right-hand side operators");
-    op->arith = mode;
-    return GBDS_SUCCESS;
-}
-
-extern "C" int gbds_op_get_arith(gbds_op op) { return op ? op->arith : -1; }
 
 extern "C" size_t gbds_op_gauge_bytes(gbds_op op) { return op ? gauge_bytes(op->g, op->prec, op->recon) : 0; }
 
@@ -273,7 +259,7 @@ extern "C" int gbds_op_pack_gauge(gbds_op op, const void *u_packed, void *gauge,
     if (reinterpret_cast<uintptr_t>(u_packed) & 7u)
         return set_error(GBDS_ERROR_INVALID_VALUE, "u_packed must be 8-byte aligned");
     cudaError_t e = launch_pack_gauge(op->g, op->prec, op->recon, u_packed, op->d_site_table, gauge,
-                                      static_cast<cudaStream_t>(stream), df_of(op));
+                                      static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_gauge");
 }
 
@@ -290,7 +276,7 @@ extern "C" int gbds_op_pack_spinor(gbds_op op, const void *psi_packed, int parit
                             : launch_pack_gen_half(op->format, op->g, op->nrhs, src, op->d_site_table, parity, spinor, st);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_spinor");
     }
-    cudaError_t e = launch_pack_spinor(op->g, op->prec, psi_packed, op->d_site_table, 0, parity, spinor, st, df_of(op));
+    cudaError_t e = launch_pack_spinor(op->g, op->prec, psi_packed, op->d_site_table, 0, parity, spinor, st);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_spinor");
 }
 
@@ -307,7 +293,7 @@ extern "C" int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity,
                             : launch_unpack_gen_half(op->format, op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "unpack_spinor");
     }
-    cudaError_t e = launch_unpack_spinor(op->g, op->prec, spinor, op->d_site_table, 0, parity, psi_packed, st, df_of(op));
+    cudaError_t e = launch_unpack_spinor(op->g, op->prec, spinor, op->d_site_table, 0, parity, psi_packed, st);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "unpack_spinor");
 }
 
@@ -328,7 +314,6 @@ extern "C" int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, vo
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
     }
     cudaError_t e = op->prec == 32 ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)
-                    : df_of(op)   ? launch_dslash_df64(op->g, op->recon, gauge, psi, res, isign, cb, nullptr, 0.0, s)
                                    : launch_dslash_f64(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
 }
@@ -358,7 +343,6 @@ int g_exit_on_error = 1;
 int g_gauge_cache = 0;
 int g_legacy_recon = 18;
 int g_host_access = 0;  // 0: read/write host arrays directly where the GPU can; 1: always stage
-int g_fp64_arith = 0;   // FP64 legacy contexts: 0 IEEE FP64, 1 float-float (set at init)
 int g_last_path = -1;   // 0 staged, 1 direct
 
 // Address under which kernels can use a caller array, or nullptr when the
@@ -460,7 +444,6 @@ void legacy_init(int prec, int nd, const int *latt_size, void (*getSiteCoords)(i
     LegacyCtx n;
     int rc = gbds_op_create(&n.op, latt_size, nd, prec, g_legacy_recon);
     if (rc == GBDS_SUCCESS && !canonical) rc = gbds_op_set_layout(n.op, table.data(), g.V);
-    if (rc == GBDS_SUCCESS && prec == 64) rc = gbds_op_set_arith(n.op, g_fp64_arith);
     if (rc != GBDS_SUCCESS) {
         std::string m = g_last_error;
         legacy_release(n);
@@ -494,13 +477,6 @@ void legacy_free(int prec, int nd) {
     if (--c.refcount == 0) legacy_release(c);
 }
 
-cudaError_t legacy_dslash(LegacyCtx &c, int prec, int isign, int cb, cudaStream_t s) {
-    const Geom &g = c.op->g;
-    if (prec == 32) return launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
-    if (c.op->arith == 1) return launch_dslash_df64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, nullptr, 0.0, s);
-    return launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
-}
-
 void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, int isign, int cb, const char *fn) {
     LegacyCtx &c = ctx_for(prec, nd);
     if (isign != 1 && isign != -1) return;  // lib/sse_su3dslash_32bit_scalar.c:162-179
@@ -522,7 +498,6 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
     const int target = 1 - cb;
     cudaStream_t s = c.stream;
     const int *table = c.op->d_site_table;
-    const int df = prec == 64 && c.op->arith == 1;
     cudaError_t e = cudaSuccess;
     const bool reuse_gauge = g_gauge_cache && c.cached_u == u;
     const void *du = nullptr, *dpsi = nullptr;
@@ -538,13 +513,14 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
         // Direct: the layout kernels read u and psi and write res where they
         // lie, with no intermediate copy.
         if (!reuse_gauge) {
-            e = launch_pack_gauge(g, prec, c.op->recon, du, nullptr, c.d_gauge, s, df);
+            e = launch_pack_gauge(g, prec, c.op->recon, du, nullptr, c.d_gauge, s);
             c.cached_u = e == cudaSuccess ? u : nullptr;
         }
-        if (e == cudaSuccess) e = launch_pack_spinor(g, prec, dpsi, nullptr, 0, cb, c.d_psi, s, df);
+        if (e == cudaSuccess) e = launch_pack_spinor(g, prec, dpsi, nullptr, 0, cb, c.d_psi, s);
         if (e == cudaSuccess)
-            e = legacy_dslash(c, prec, isign, cb, s);
-        if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, nullptr, 0, target, dres, s, df);
+            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s)
+                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
+        if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, nullptr, 0, target, dres, s);
         cudaError_t e2 = cudaStreamSynchronize(s);
         if (e == cudaSuccess) e = e2;
         g_last_path = 1;
@@ -557,17 +533,18 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
     g_last_path = 0;
     if (!reuse_gauge) {
         e = cudaMemcpyAsync(c.d_u_packed, u, (size_t)g.V * 4 * 18 * real, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = launch_pack_gauge(g, prec, c.op->recon, c.d_u_packed, table, c.d_gauge, s, df);
+        if (e == cudaSuccess) e = launch_pack_gauge(g, prec, c.op->recon, c.d_u_packed, table, c.d_gauge, s);
         c.cached_u = e == cudaSuccess ? u : nullptr;
     }
     if (c.canonical) {
         // Checkerboards are contiguous halves of the caller's arrays.
         const char *src = static_cast<const char *>(psi) + (size_t)cb * g.Vh * spinor;
         if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_psi_packed, src, (size_t)g.Vh * spinor, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = launch_pack_spinor(g, prec, c.d_psi_packed, nullptr, cb * g.Vh, cb, c.d_psi, s, df);
+        if (e == cudaSuccess) e = launch_pack_spinor(g, prec, c.d_psi_packed, nullptr, cb * g.Vh, cb, c.d_psi, s);
         if (e == cudaSuccess)
-            e = legacy_dslash(c, prec, isign, cb, s);
-        if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, nullptr, target * g.Vh, target, c.d_res_packed, s, df);
+            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s)
+                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
+        if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, nullptr, target * g.Vh, target, c.d_res_packed, s);
         char *dst = static_cast<char *>(res) + (size_t)target * g.Vh * spinor;
         if (e == cudaSuccess) e = cudaMemcpyAsync(dst, c.d_res_packed, (size_t)g.Vh * spinor, cudaMemcpyDeviceToHost, s);
     } else {
@@ -575,10 +552,11 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
         // of `res` are carried through unchanged.
         if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_psi_packed, psi, (size_t)g.V * spinor, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_res_packed, res, (size_t)g.V * spinor, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = launch_pack_spinor(g, prec, c.d_psi_packed, table, 0, cb, c.d_psi, s, df);
+        if (e == cudaSuccess) e = launch_pack_spinor(g, prec, c.d_psi_packed, table, 0, cb, c.d_psi, s);
         if (e == cudaSuccess)
-            e = legacy_dslash(c, prec, isign, cb, s);
-        if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, table, 0, target, c.d_res_packed, s, df);
+            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s)
+                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block, c.op->variant, s);
+        if (e == cudaSuccess) e = launch_unpack_spinor(g, prec, c.d_res, table, 0, target, c.d_res_packed, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(res, c.d_res_packed, (size_t)g.V * spinor, cudaMemcpyDeviceToHost, s);
     }
     cudaError_t e2 = cudaStreamSynchronize(s);
@@ -670,12 +648,6 @@ extern "C" int gbds_legacy_set_host_access(int mode) {
 }
 
 extern "C" int gbds_legacy_last_path(void) { return g_last_path; }
-
-extern "C" int gbds_legacy_set_fp64_arith(int mode) {
-    if (mode != GBDS_ARITH_IEEE && mode != GBDS_ARITH_DF64) return set_error(GBDS_ERROR_INVALID_VALUE, "unknown arithmetic mode");
-    g_fp64_arith = mode;
-    return GBDS_SUCCESS;
-}
 
 extern "C" int gbds_legacy_refcount(int prec, int nd) {
     if ((prec != 32 && prec != 64) || (nd != 3 && nd != 4)) return -1;

@@ -45,19 +45,12 @@ cudaError_t launch_dslash_xpay_f64(const Geom &g, int recon, const void *gauge, 
                                    double coef, void *res, double *partials, int isign, int cb, cudaStream_t stream);
 
 // site0: first caller site held by the packed buffer (0 for a full lattice).
-// df (prec 64 only): the internal field holds float-float pairs (df64), so
-// the kernels convert from / to the packed IEEE doubles on the way.
 cudaError_t launch_pack_spinor(const Geom &g, int prec, const void *psi_packed, const int *site_table,
-                               int site0, int parity, void *spinor, cudaStream_t stream, int df = 0);
+                               int site0, int parity, void *spinor, cudaStream_t stream);
 cudaError_t launch_unpack_spinor(const Geom &g, int prec, const void *spinor, const int *site_table,
-                                 int site0, int parity, void *psi_packed, cudaStream_t stream, int df = 0);
+                                 int site0, int parity, void *psi_packed, cudaStream_t stream);
 cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_packed,
-                              const int *site_table, void *gauge, cudaStream_t stream, int df = 0);
-// FP64-class Dslash in float-float arithmetic on df64 fields (dslash_df64.cu);
-// x != nullptr: res = x + coef * D psi.
-cudaError_t launch_dslash_df64(const Geom &g, int recon, const void *gauge, const void *psi, void *res, int isign, int cb,
-                               const void *x, double coef, cudaStream_t st);
-cudaError_t convert_df64(void *field, size_t n, int to_df, cudaStream_t st);
+                              const int *site_table, void *gauge, cudaStream_t stream);
 
 // Generalised Dslash (dslash_gen_*.cu): FP32 arithmetic and links, nrhs in
 // {1,2,4,8,16,32}, spinor formats 0 FP32, 1 BF16, 2 FP16 + norm.  x != nullptr
@@ -93,7 +86,6 @@ struct gbds_op_s {
     int recon;
     int block;
     int variant;
-    int arith;   // prec 64: 0 IEEE FP64, 1 float-float (df64) fields and arithmetic
     int nrhs;    // right-hand sides per site (1 = the plain operator)
     int format;  // spinor storage: 0 native (prec), 1 bfloat16, 2 half + per-spinor norm
     int *d_site_table;  // device copy of the layout table, or nullptr (canonical)

@@ -15,55 +15,34 @@ namespace gbds {
 
 namespace {
 
-// One complex, 16 bytes: IEEE double2 <-> float-float {re.hi, re.lo, im.hi, im.lo}.
-__device__ __forceinline__ uint4 to_df_unit(uint4 u) {
-    double2 d;
-    memcpy(&d, &u, 16);
-    const float rh = __double2float_rn(d.x), ih = __double2float_rn(d.y);
-    const float4 f = make_float4(rh, __double2float_rn(d.x - (double)rh), ih, __double2float_rn(d.y - (double)ih));
-    uint4 r;
-    memcpy(&r, &f, 16);
-    return r;
-}
-__device__ __forceinline__ uint4 from_df_unit(uint4 u) {
-    float4 f;
-    memcpy(&f, &u, 16);
-    const double2 d = make_double2((double)f.x + (double)f.y, (double)f.z + (double)f.w);
-    uint4 r;
-    memcpy(&r, &d, 16);
-    return r;
-}
-
 // Spinors move as 16-byte units: FP32 = 6 units (float4), FP64 = 12 (double2).
 // `site0` is subtracted from the caller index before addressing `packed`, so
 // a buffer that holds only sites [site0, site0 + Vh) can be used.
 __global__ void pack_spinor_kernel(const uint4 *__restrict__ packed, const int *__restrict__ table, int site0,
-                                   int parity, int Vh, int stride, int units, uint4 *__restrict__ soa, int df) {
+                                   int parity, int Vh, int stride, int units, uint4 *__restrict__ soa) {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= (long long)units * Vh) return;
     const int k = (int)(tid / Vh), h = (int)(tid % Vh);
     const int i = parity * Vh + h;
     const int c = table ? __ldg(table + i) : i;
-    const uint4 v = __ldg(packed + (size_t)(c - site0) * units + k);
-    soa[(size_t)k * stride + h] = df ? to_df_unit(v) : v;
+    soa[(size_t)k * stride + h] = __ldg(packed + (size_t)(c - site0) * units + k);
 }
 
 __global__ void unpack_spinor_kernel(const uint4 *__restrict__ soa, const int *__restrict__ table, int site0,
-                                     int parity, int Vh, int stride, int units, uint4 *__restrict__ packed, int df) {
+                                     int parity, int Vh, int stride, int units, uint4 *__restrict__ packed) {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= (long long)units * Vh) return;
     const int h = (int)(tid / units), k = (int)(tid % units);
     const int i = parity * Vh + h;
     const int c = table ? __ldg(table + i) : i;
-    const uint4 v = __ldg(soa + (size_t)k * stride + h);
-    packed[(size_t)(c - site0) * units + k] = df ? from_df_unit(v) : v;
+    packed[(size_t)(c - site0) * units + k] = __ldg(soa + (size_t)k * stride + h);
 }
 
 // One thread per (parity, mu, h): reads the packed 3x3 link (transposed,
 // u[j][i] = U_ij), writes the internal components.
 template <typename T, int RECON>
 __global__ void pack_gauge_kernel(const T *__restrict__ packed, const int *__restrict__ table,
-                                  Geom g, char *__restrict__ gauge, size_t block_bytes, int df) {
+                                  Geom g, char *__restrict__ gauge, size_t block_bytes) {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = 2LL * g.nd * g.Vh;
     if (tid >= n) return;
@@ -95,15 +74,10 @@ __global__ void pack_gauge_kernel(const T *__restrict__ packed, const int *__res
                                                       U[b / 3][b % 3][0], U[b / 3][b % 3][1]);
         }
     } else {
-        uint4 *d = reinterpret_cast<uint4 *>(blk);
+        double2 *d = reinterpret_cast<double2 *>(blk);
         constexpr int nk = RECON == 18 ? 9 : 6;
 #pragma unroll
-        for (int k = 0; k < nk; k++) {
-            const double2 v = make_double2(U[k / 3][k % 3][0], U[k / 3][k % 3][1]);
-            uint4 u;
-            memcpy(&u, &v, 16);
-            d[(size_t)k * g.stride + h] = df ? to_df_unit(u) : u;
-        }
+        for (int k = 0; k < nk; k++) d[(size_t)k * g.stride + h] = make_double2(U[k / 3][k % 3][0], U[k / 3][k % 3][1]);
     }
 }
 
@@ -122,8 +96,7 @@ constexpr int kGaugeTile = 32;
 
 // packed: first site of checkerboard `parity` (sites [0, Vh) of that half).
 template <int UNITS>
-__global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int Vh, int stride, uint4 *__restrict__ soa,
-                                                        int df) {
+__global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int Vh, int stride, uint4 *__restrict__ soa) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
     const int h0 = blockIdx.x * kSpinorTile;
     const int n = min(kSpinorTile, Vh - h0);
@@ -132,21 +105,18 @@ __global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int
     __syncthreads();
     for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
         const int k = e / n, t = e - k * n;
-        const uint4 v = sm[t * UNITS + k];
-        soa[(size_t)k * stride + h0 + t] = df ? to_df_unit(v) : v;
+        soa[(size_t)k * stride + h0 + t] = sm[t * UNITS + k];
     }
 }
 
 template <int UNITS>
-__global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restrict__ soa, int Vh, int stride, uint4 *packed,
-                                                          int df) {
+__global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restrict__ soa, int Vh, int stride, uint4 *packed) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
     const int h0 = blockIdx.x * kSpinorTile;
     const int n = min(kSpinorTile, Vh - h0);
     for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
         const int k = e / n, t = e - k * n;
-        const uint4 v = __ldg(soa + (size_t)k * stride + h0 + t);
-        sm[t * UNITS + k] = df ? from_df_unit(v) : v;
+        sm[t * UNITS + k] = __ldg(soa + (size_t)k * stride + h0 + t);
     }
     __syncthreads();
     uint4 *dst = packed + (size_t)h0 * UNITS;
@@ -158,7 +128,7 @@ __global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restric
 // bytes (one float2 / one double) keep the 3D skip of mu = 3 exact.
 template <typename T, int RECON>
 __global__ void __launch_bounds__(128) pack_gauge_tile(const unsigned long long *packed, Geom g, char *__restrict__ gauge,
-                                                        size_t block_bytes, int df) {
+                                                        size_t block_bytes) {
     constexpr int SITE_UNITS = 4 * 18 * sizeof(T) / 8;  // 8-byte units per site (4 links)
     constexpr int LINK_UNITS = 18 * sizeof(T) / 8;
     __shared__ unsigned long long sm[kGaugeTile * SITE_UNITS];
@@ -190,10 +160,7 @@ __global__ void __launch_bounds__(128) pack_gauge_tile(const unsigned long long 
                             m[(3 * (b % 3) + b / 3) * 2], m[(3 * (b % 3) + b / 3) * 2 + 1]);
         } else {
             const int r = k / 3, c = k % 3;
-            const double2 v = make_double2(m[(3 * c + r) * 2], m[(3 * c + r) * 2 + 1]);
-            uint4 u;
-            memcpy(&u, &v, 16);
-            reinterpret_cast<uint4 *>(blk)[(size_t)k * g.stride + h] = df ? to_df_unit(u) : u;
+            reinterpret_cast<double2 *>(blk)[(size_t)k * g.stride + h] = make_double2(m[(3 * c + r) * 2], m[(3 * c + r) * 2 + 1]);
         }
     }
 }
@@ -209,46 +176,46 @@ size_t gauge_block_bytes(const Geom &g, int prec, int recon) {
 size_t gauge_bytes(const Geom &g, int prec, int recon) { return 2 * (size_t)g.nd * gauge_block_bytes(g, prec, recon); }
 
 cudaError_t launch_pack_spinor(const Geom &g, int prec, const void *psi_packed, const int *site_table,
-                               int site0, int parity, void *spinor, cudaStream_t stream, int df) {
+                               int site0, int parity, void *spinor, cudaStream_t stream) {
     const int units = prec == 32 ? 6 : 12;
     if (!site_table) {
         // canonical: the checkerboard is the contiguous run [parity*Vh, parity*Vh + Vh) - site0
         const uint4 *src = static_cast<const uint4 *>(psi_packed) + (size_t)(parity * g.Vh - site0) * units;
         const unsigned nb = blocks_for(g.Vh, kSpinorTile);
-        if (prec == 32) pack_spinor_tile<6><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, static_cast<uint4 *>(spinor), 0);
-        else pack_spinor_tile<12><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, static_cast<uint4 *>(spinor), df);
+        if (prec == 32) pack_spinor_tile<6><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, static_cast<uint4 *>(spinor));
+        else pack_spinor_tile<12><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, static_cast<uint4 *>(spinor));
         count_launch();
         return cudaGetLastError();
     }
     const long long n = (long long)units * g.Vh;
     pack_spinor_kernel<<<blocks_for(n, 256), 256, 0, stream>>>(static_cast<const uint4 *>(psi_packed), site_table,
                                                                site0, parity, g.Vh, g.stride, units,
-                                                               static_cast<uint4 *>(spinor), prec == 64 ? df : 0);
+                                                               static_cast<uint4 *>(spinor));
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_unpack_spinor(const Geom &g, int prec, const void *spinor, const int *site_table,
-                                 int site0, int parity, void *psi_packed, cudaStream_t stream, int df) {
+                                 int site0, int parity, void *psi_packed, cudaStream_t stream) {
     const int units = prec == 32 ? 6 : 12;
     if (!site_table) {
         uint4 *dst = static_cast<uint4 *>(psi_packed) + (size_t)(parity * g.Vh - site0) * units;
         const unsigned nb = blocks_for(g.Vh, kSpinorTile);
-        if (prec == 32) unpack_spinor_tile<6><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), g.Vh, g.stride, dst, 0);
-        else unpack_spinor_tile<12><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), g.Vh, g.stride, dst, df);
+        if (prec == 32) unpack_spinor_tile<6><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), g.Vh, g.stride, dst);
+        else unpack_spinor_tile<12><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), g.Vh, g.stride, dst);
         count_launch();
         return cudaGetLastError();
     }
     const long long n = (long long)units * g.Vh;
     unpack_spinor_kernel<<<blocks_for(n, 256), 256, 0, stream>>>(static_cast<const uint4 *>(spinor), site_table,
                                                                  site0, parity, g.Vh, g.stride, units,
-                                                                 static_cast<uint4 *>(psi_packed), prec == 64 ? df : 0);
+                                                                 static_cast<uint4 *>(psi_packed));
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_packed, const int *site_table,
-                              void *gauge, cudaStream_t stream, int df) {
+                              void *gauge, cudaStream_t stream) {
     const long long n = 2LL * g.nd * g.Vh;
     const size_t bb = gauge_block_bytes(g, prec, recon);
     char *dst = static_cast<char *>(gauge);
@@ -256,11 +223,11 @@ cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_
         const unsigned long long *src = static_cast<const unsigned long long *>(u_packed);
         const unsigned nt = blocks_for(g.V, kGaugeTile);
         if (prec == 32) {
-            if (recon == 18) pack_gauge_tile<float, 18><<<nt, 128, 0, stream>>>(src, g, dst, bb, 0);
-            else pack_gauge_tile<float, 12><<<nt, 128, 0, stream>>>(src, g, dst, bb, 0);
+            if (recon == 18) pack_gauge_tile<float, 18><<<nt, 128, 0, stream>>>(src, g, dst, bb);
+            else pack_gauge_tile<float, 12><<<nt, 128, 0, stream>>>(src, g, dst, bb);
         } else {
-            if (recon == 18) pack_gauge_tile<double, 18><<<nt, 128, 0, stream>>>(src, g, dst, bb, df);
-            else pack_gauge_tile<double, 12><<<nt, 128, 0, stream>>>(src, g, dst, bb, df);
+            if (recon == 18) pack_gauge_tile<double, 18><<<nt, 128, 0, stream>>>(src, g, dst, bb);
+            else pack_gauge_tile<double, 12><<<nt, 128, 0, stream>>>(src, g, dst, bb);
         }
         count_launch();
         return cudaGetLastError();
@@ -268,12 +235,12 @@ cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_
     const unsigned nb = blocks_for(n, 128);
     if (prec == 32) {
         const float *src = static_cast<const float *>(u_packed);
-        if (recon == 18) pack_gauge_kernel<float, 18><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb, 0);
-        else pack_gauge_kernel<float, 12><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb, 0);
+        if (recon == 18) pack_gauge_kernel<float, 18><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb);
+        else pack_gauge_kernel<float, 12><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb);
     } else {
         const double *src = static_cast<const double *>(u_packed);
-        if (recon == 18) pack_gauge_kernel<double, 18><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb, df);
-        else pack_gauge_kernel<double, 12><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb, df);
+        if (recon == 18) pack_gauge_kernel<double, 18><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb);
+        else pack_gauge_kernel<double, 12><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb);
     }
     count_launch();
     return cudaGetLastError();

@@ -82,10 +82,6 @@ class DslashOperator:
     def canonical(self) -> bool:
         return bool(_lib.core().gbds_op_is_canonical(self._h))
 
-    def set_arith(self, mode: str) -> None:
-        """prec 64 only: "ieee" (default) or "df64" (float-float on the FP32 units)."""
-        _lib.check(_lib.core().gbds_op_set_arith(self._h, {"ieee": 0, "df64": 1}[mode]))
-
     def set_tuning(self, threads: int, variant: int = 0) -> None:
         _lib.check(_lib.core().gbds_op_set_tuning(self._h, int(threads), int(variant)))
 

@@ -112,11 +112,6 @@ def set_host_access(mode: int) -> None:
     _lib.check(_lib.core().gbds_legacy_set_host_access(int(mode)))
 
 
-def set_fp64_arith(mode: str) -> None:
-    """FP64 contexts created by later inits: "ieee" (default) or "df64"."""
-    _lib.check(_lib.core().gbds_legacy_set_fp64_arith({"ieee": 0, "df64": 1}[mode]))
-
-
 def last_path() -> int:
     """1 if the last apply used direct host access, 0 if it staged copies."""
     return int(_lib.core().gbds_legacy_last_path())

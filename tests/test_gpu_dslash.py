@@ -36,24 +36,19 @@ def _apply(d, nd, u, psi, res, isign, cb):
     (d.sse_su3dslash_wilson if nd == 4 else d.sse_su3dslash_wilson_3d)(u, psi, res, isign, cb)
 
 
-@pytest.mark.parametrize("recon,access,arith", [(18, 0, "ieee"), (18, 1, "ieee"), (12, 0, "ieee"), (18, 0, "df64"),
-                                               (12, 1, "df64")])
+@pytest.mark.parametrize("recon,access", [(18, 0), (18, 1), (12, 0)])
 @pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("name", CASES)
-def test_dropin_matches_reference_golden(dropin, name, prec, recon, access, arith):
+def test_dropin_matches_reference_golden(dropin, name, prec, recon, access):
     """access 0: kernels read/write the host arrays directly where the GPU can
-    reach them; 1: staged through cudaMemcpyAsync.  arith df64: the FP64
-    library in float-float arithmetic, held to the same FP64 tolerance."""
+    reach them; 1: staged through cudaMemcpyAsync."""
     from sse_wilson_dslash_gb300 import legacy
-    if arith == "df64" and prec == 32:
-        pytest.skip("float-float is an FP64 mode")
     c = MAN["cases"][name]
     dims, nd = tuple(c["dims"]), c["nd"]
     kind, lol = layout(c, dims)
     d = dropin[prec]
     legacy.set_recon(recon)
     legacy.set_host_access(access)
-    legacy.set_fp64_arith(arith)
     try:
         _init(d, nd, dims, kind, lol)
         u, psi = O.make_inputs(dims, MAN["seeds"]["gauge"], MAN["seeds"]["spinor"], c["gauge"])
@@ -75,7 +70,6 @@ def test_dropin_matches_reference_golden(dropin, name, prec, recon, access, arit
         _free(d, nd)
         legacy.set_recon(18)
         legacy.set_host_access(0)
-        legacy.set_fp64_arith("ieee")
 
 
 def test_refcount_keeps_first_lattice(dropin):
@@ -206,18 +200,13 @@ def _device_fields(op, u, psi, torch):
 
 
 @pytest.mark.parametrize("recon", [18, 12])
-@pytest.mark.parametrize("prec", [32, 64, "df64"])
+@pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("nd,dims,layout_kind", [(4, (8, 4, 6, 4), "canonical"), (3, (4, 6, 4, 5), "canonical"),
                                                   (4, (4, 4, 2, 6), "scrambled"), (3, (4, 2, 4, 3), "scrambled")])
 def test_device_operator(nd, dims, layout_kind, prec, recon):
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
-    arith = "ieee"
-    if prec == "df64":
-        prec, arith = 64, "df64"
     op = DslashOperator(dims, nd=nd, prec=prec, recon=recon)
-    if arith == "df64":
-        op.set_arith("df64")
     V = op.volume
     if layout_kind == "canonical":
         lol = O.layout_table(O.LAYOUT_CB2 if nd == 4 else O.LAYOUT_CB3D, dims)
