@@ -171,8 +171,9 @@ def run_solver_bench(torch, log_fn):
     out = {"lattice": list(dims), "kappa": 0.124, "links": "exp(i 0.3 H), H traceless Hermitian N(0,1)",
            "source": "N(0,1)", "tol": 1e-10, "residual": "|M^+ b - M^+ M x| / |M^+ b| (CG on M^+ M)"}
     sols = {}
-    for name, prec, recon in (("fp64_cg", 64, 18), ("mixed_fp32_fp64", 32, 12)):
-        s = WilsonSolver(dims, 0.124, tol=1e-10, max_iter=20000, inner_prec=prec, inner_recon=recon, inner_tol=1e-5)
+    for name, prec, recon, itol in (("fp64_cg", 64, 18, 1e-5), ("mixed_fp32_fp64", 32, 12, 1e-5),
+                                    ("mixed_fp16_fp64", 16, 12, 1e-3), ("mixed_bf16_fp64", 17, 12, 1e-3)):
+        s = WilsonSolver(dims, 0.124, tol=1e-10, max_iter=20000, inner_prec=prec, inner_recon=recon, inner_tol=itol)
         s.set_gauge(u)
         x = torch.zeros_like(b)
         torch.cuda.synchronize()
@@ -188,7 +189,9 @@ def run_solver_bench(torch, log_fn):
         del s
         torch.cuda.empty_cache()
     out["speedup"] = out["fp64_cg"]["wall_seconds"] / out["mixed_fp32_fp64"]["wall_seconds"]
-    out["solution_rel_diff"] = float((sols["fp64_cg"] - sols["mixed_fp32_fp64"]).norm() / sols["fp64_cg"].norm())
+    for k in ("mixed_fp32_fp64", "mixed_fp16_fp64", "mixed_bf16_fp64"):
+        out[k]["speedup_vs_fp64"] = out["fp64_cg"]["wall_seconds"] / out[k]["wall_seconds"]
+        out[k]["solution_rel_diff"] = float((sols["fp64_cg"] - sols[k]).norm() / sols["fp64_cg"].norm())
     return out
 
 

@@ -253,7 +253,10 @@ typedef struct gbds_solver_params {
     double kappa;     /* hopping parameter */
     double tol;       /* stop when |c - A x| <= tol |c| (FP64) */
     int max_iter;     /* CG iterations, all cycles together */
-    int inner_prec;   /* 64: all-FP64 CG; 32: FP32 CG inside FP64 defect correction */
+    int inner_prec;   /* 64: all-FP64 CG; 32: FP32 CG inside FP64 defect correction;
+                         16 / 17: as 32 with the CG direction and operator
+                         intermediates in half + per-site norm (16) or
+                         bfloat16 (17), FP16 links, FP32 arithmetic */
     int inner_recon;  /* 18 or 12: gauge compression of the FP32 operator */
     double inner_tol; /* residual reduction per defect-correction cycle (e.g. 1e-5) */
 } gbds_solver_params;

@@ -131,6 +131,35 @@ struct Sio<kFmtF16N> {
     }
 };
 
+// Link loads: LFMT 0 = FP32 (float2 x 9 or float4 x 3), LFMT 1 = FP16 with the
+// same component grouping (half2 x 9 or 4 x half in a uint2, x 3).  SU(3)
+// entries are bounded by 1, so half needs no scaling.
+template <int LFMT, int RECON>
+__device__ __forceinline__ void load_link_g(const char *base, int stride, int h, cx<float> (&U)[3][3]) {
+    if constexpr (LFMT == 0) {
+        Field<float>::template load_link<RECON>(base, stride, h, U);
+    } else if constexpr (RECON == 18) {
+        const unsigned *p = reinterpret_cast<const unsigned *>(base);
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const unsigned w = __ldg(p + (size_t)k * stride + h);
+            const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w));
+            U[k / 3][k % 3] = {f.x, f.y};
+        }
+    } else {
+        const uint2 *p = reinterpret_cast<const uint2 *>(base);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint2 q = __ldg(p + (size_t)k * stride + h);
+            const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&q.x));
+            const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&q.y));
+            U[(2 * k) / 3][(2 * k) % 3] = {a.x, a.y};
+            U[(2 * k + 1) / 3][(2 * k + 1) % 3] = {b.x, b.y};
+        }
+        reconstruct_row2(U);
+    }
+}
+
 struct GenArgs {
     Geom g;
     const char *psi;           // source checkerboard
@@ -150,25 +179,25 @@ struct GenArgs {
 template <int NRHS>
 __device__ __forceinline__ int nrhs_of(const GenArgs &a) { return NRHS > 0 ? NRHS : a.nrhs; }
 
-template <int FMT, int RECON, int ISIGN, int NRHS, int MU>
+template <int FMT, int RECON, int ISIGN, int NRHS, int MU, int LFMT>
 __device__ __forceinline__ void gen_hop_pair(const GenArgs &a, int h, int r, const Nbr &n, cx<float> (&acc)[4][3]) {
     const int ps = 1 - a.pt;
     const int nr = nrhs_of<NRHS>(a);
     cx<float> s[4][3], hs[2][3], w[2][3], U[3][3];
     Sio<FMT>::load(a.psi, a.cs, (size_t)n.f[MU] * nr + r, s);
-    Field<float>::template load_link<RECON>(a.gauge + (size_t)(a.pt * 4 + MU) * a.link_block_bytes, a.g.stride, h, U);
+    load_link_g<LFMT, RECON>(a.gauge + (size_t)(a.pt * 4 + MU) * a.link_block_bytes, a.g.stride, h, U);
     project<MU, ISIGN>(s, hs);
     su3_mul<false>(U, hs, w);
     reconstruct<MU, ISIGN>(acc, w);
     Sio<FMT>::load(a.psi, a.cs, (size_t)n.b[MU] * nr + r, s);
-    Field<float>::template load_link<RECON>(a.gauge + (size_t)(ps * 4 + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
+    load_link_g<LFMT, RECON>(a.gauge + (size_t)(ps * 4 + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
     project<MU, -ISIGN>(s, hs);
     su3_mul<true>(U, hs, w);
     reconstruct<MU, -ISIGN>(acc, w);
 }
 
 // One thread per (site, rhs); 4D.  EPI = 1 adds the xpay epilogue.
-template <int FMT, int RECON, int ISIGN, int NRHS, int EPI>
+template <int FMT, int RECON, int ISIGN, int NRHS, int EPI, int LFMT = 0>
 __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nr = nrhs_of<NRHS>(a);
@@ -182,10 +211,10 @@ __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
         for (int s = 0; s < 4; s++)
 #pragma unroll
             for (int c = 0; c < 3; c++) acc[s][c] = {0.f, 0.f};
-        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 0>(a, h, r, n, acc);
-        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 1>(a, h, r, n, acc);
-        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 2>(a, h, r, n, acc);
-        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 3>(a, h, r, n, acc);
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 0, LFMT>(a, h, r, n, acc);
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 1, LFMT>(a, h, r, n, acc);
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 2, LFMT>(a, h, r, n, acc);
+        gen_hop_pair<FMT, RECON, ISIGN, NRHS, 3, LFMT>(a, h, r, n, acc);
         const size_t i = (size_t)h * nr + r;
         if constexpr (EPI) {
             cx<float> xv[4][3];

@@ -53,6 +53,36 @@ void launch_gen_nrhs(const GenArgs &a, int nrhs, dim3 grid, cudaStream_t st) {
     }
 }
 
+// nrhs 1 with FP16 links (the 16-bit inner solver's operator)
+template <int FMT>
+cudaError_t launch_gen_h16_t(const Geom &g, int recon, const void *gauge, const void *psi, void *res, int isign, int cb,
+                             const void *x, float coef, double *partials, cudaStream_t st) {
+    GenArgs a;
+    a.g = g;
+    a.psi = static_cast<const char *>(psi);
+    a.res = static_cast<char *>(res);
+    a.gauge = static_cast<const char *>(gauge);
+    a.link_block_bytes = (size_t)recon * 2 * g.stride;
+    a.cs = (size_t)g.stride;
+    a.nrhs = 1;
+    a.pt = 1 - cb;
+    a.x = static_cast<const char *>(x);
+    a.coef = coef;
+    a.partials = partials;
+    const dim3 grid((unsigned)((g.Vh + 127) / 128));
+#define GBDS_H(R, S, E) dslash_gen_kernel<FMT, R, S, 1, E, 1><<<grid, 128, 0, st>>>(a)
+    if (x) {
+        if (recon == 18) { if (isign > 0) GBDS_H(18, 1, 1); else GBDS_H(18, -1, 1); }
+        else             { if (isign > 0) GBDS_H(12, 1, 1); else GBDS_H(12, -1, 1); }
+    } else {
+        if (recon == 18) { if (isign > 0) GBDS_H(18, 1, 0); else GBDS_H(18, -1, 0); }
+        else             { if (isign > 0) GBDS_H(12, 1, 0); else GBDS_H(12, -1, 0); }
+    }
+#undef GBDS_H
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <int FMT>
 cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
                          int cb, const void *x, float coef, double *partials, cudaStream_t st) {

@@ -70,6 +70,12 @@ cudaError_t launch_pack_gen_half(int fmt, const Geom &g, int nrhs, const float *
 cudaError_t launch_unpack_gen_half(int fmt, const Geom &g, int nrhs, const void *in, const int *table, int parity,
                                    float *packed, cudaStream_t st);
 inline int gen_spinor_bytes(int fmt) { return fmt == 0 ? 96 : (fmt == 1 ? 48 : 52); }
+// nrhs 1, 16-bit spinors (fmt 1 / 2) with FP16 links: gauge is the FP32
+// internal gauge converted by convert_links_f16 (recon * 2 bytes per link
+// per site-stride).
+cudaError_t launch_gen_h16(int fmt, const Geom &g, int recon, const void *gauge, const void *psi, void *res, int isign,
+                           int cb, const void *x, float coef, double *partials, cudaStream_t st);
+cudaError_t convert_links_f16(const void *gauge32, void *gauge16, size_t nfloats, cudaStream_t st);
 
 // Sizes in bytes of the internal fields.
 size_t spinor_bytes(const Geom &g, int prec);

@@ -10,6 +10,10 @@
 //                  FP64) inside FP64 defect correction: the residual
 //                  r = c - A x, the solution update x += |r| e and all global
 //                  norms stay in FP64 on the GPU.
+//   inner_prec 16 / 17: the same with the CG's direction p and the operator's
+//                  intermediates (M p, A p, D_oe p) stored as half with a
+//                  per-site norm (16) or bfloat16 (17), FP16 links, FP32
+//                  arithmetic; the CG's solution and residual stay FP32.
 // The reference library provides only D; a caller such as Chroma builds M and
 // its solvers around it (tests/dslashm_w.cc states D the same way).  Scalars
 // of the iteration (rr, pAp, alpha, beta) live in device memory and are
@@ -21,7 +25,7 @@
 #include <cmath>
 #include <cstdio>
 
-#include "dslash_kernel.cuh"
+#include "dslash_gen.cuh"
 
 namespace gbds {
 namespace {
@@ -163,6 +167,76 @@ __global__ void __launch_bounds__(kThreads) promote_update(const float4 *__restr
     }
 }
 
+// --- 16-bit direction vectors (Sio formats), FP32 solution and residual ---
+
+// float4 component k of a spinor holds complexes 2k and 2k+1
+__device__ __forceinline__ float4 pair(const cx<float> (&s)[4][3], int k) {
+    const cx<float> a = s[(2 * k) / 3][(2 * k) % 3], b = s[(2 * k + 1) / 3][(2 * k + 1) % 3];
+    return make_float4(a.r, a.i, b.r, b.i);
+}
+
+// x += alpha p;  r -= alpha Ap;  partial |r|^2   (p, Ap 16-bit)
+template <int FMT>
+__global__ void __launch_bounds__(kThreads) cg_update_h(float4 *x, float4 *r, const char *p, const char *Ap,
+                                                       const Scalars *sc, int Vh, int stride, double *partials) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    float nrm = 0.f;
+    if (h < Vh) {
+        const float a = (float)sc->alpha;
+        cx<float> ps[4][3], aps[4][3];
+        Sio<FMT>::load(p, stride, h, ps);
+        Sio<FMT>::load(Ap, stride, h, aps);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const size_t i = (size_t)k * stride + h;
+            x[i] = axpy_v(a, pair(ps, k), x[i]);
+            const float4 rn = axpy_v(-a, pair(aps, k), r[i]);
+            r[i] = rn;
+            nrm += norm_v(rn);
+        }
+    }
+    block_sum_to<float>(partials, nrm);
+}
+
+// p = r + beta p   (p 16-bit)
+template <int FMT>
+__global__ void __launch_bounds__(kThreads) cg_xpay_h(const float4 *__restrict__ r, char *p, const Scalars *sc, int Vh,
+                                                     int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+    const float b = (float)sc->beta;
+    cx<float> ps[4][3];
+    Sio<FMT>::load(p, stride, h, ps);
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float4 rv = r[(size_t)k * stride + h];
+        cx<float> &u = ps[(2 * k) / 3][(2 * k) % 3];
+        cx<float> &v = ps[(2 * k + 1) / 3][(2 * k + 1) % 3];
+        u = {fmaf(b, u.r, rv.x), fmaf(b, u.i, rv.y)};
+        v = {fmaf(b, v.r, rv.z), fmaf(b, v.i, rv.w)};
+    }
+    Sio<FMT>::store(p, stride, h, ps);
+}
+
+// r32 = r64 / sqrt(outer_rr);  p = r32 (16-bit)
+template <int FMT>
+__global__ void __launch_bounds__(kThreads) demote_residual_h(const double2 *__restrict__ r64, float4 *r32, char *p,
+                                                             const Scalars *sc, int Vh, int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+    const double s = 1.0 / sqrt(sc->outer_rr);
+    cx<float> ps[4][3];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const double2 a = r64[(size_t)(2 * k) * stride + h], b = r64[(size_t)(2 * k + 1) * stride + h];
+        const float4 f = make_float4((float)(a.x * s), (float)(a.y * s), (float)(b.x * s), (float)(b.y * s));
+        r32[(size_t)k * stride + h] = f;
+        ps[(2 * k) / 3][(2 * k) % 3] = {f.x, f.y};
+        ps[(2 * k + 1) / 3][(2 * k + 1) % 3] = {f.z, f.w};
+    }
+    Sio<FMT>::store(p, stride, h, ps);
+}
+
 enum FinishMode { kAlpha = 0, kBeta = 1, kSetRR = 2, kOuterRR = 3, kNorm = 4 };
 
 // Deterministic sum of the block partials (fixed order), then the scalar step.
@@ -207,6 +281,9 @@ struct gbds_solver_s {
          *Mp64 = nullptr, *t64 = nullptr;
     // FP32 inner fields
     void *e32 = nullptr, *r32 = nullptr, *p32 = nullptr, *Ap32 = nullptr, *Mp32 = nullptr, *t32 = nullptr;
+    // 16-bit inner fields and FP16 links (inner_prec 16 / 17)
+    void *p16 = nullptr, *Ap16 = nullptr, *Mp16 = nullptr, *t16 = nullptr, *gauge16 = nullptr;
+    int fmt16 = 0;
     double *partials = nullptr;
     Scalars *sc = nullptr;    // device
     Scalars *hsc = nullptr;   // pinned host copy
@@ -250,6 +327,18 @@ cudaError_t apply_M(gbds_solver s, const void *gauge, int recon, const void *in,
     return dslash_xpay<T>(g, recon, gauge, tmp, in, (T)(-k2), out, partials, isign, 1, st);
 }
 
+// A low-precision inner solve whose residual has not dropped below 0.9 of its
+// best value for 96 iterations has reached the accuracy its storage allows:
+// the defect correction takes over from there.
+bool stagnated(double rr, int k, double &best, int &best_k) {
+    if (rr < 0.81 * best) {
+        best = rr;
+        best_k = k;
+        return false;
+    }
+    return k - best_k >= 96;
+}
+
 cudaError_t read_scalars(gbds_solver s, cudaStream_t st) {
     cudaError_t e = cudaMemcpyAsync(s->hsc, s->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -266,6 +355,8 @@ cudaError_t cg(gbds_solver s, const void *gauge, int recon, void *x, void *r, vo
     const int check_every = sizeof(T) == 4 ? 4 : 1;
     cudaError_t e = cudaSuccess;
     int k = 0;
+    double best = 1e300;
+    int best_k = 0;
     while (k < max_iter) {
         e = apply_M<T>(s, gauge, recon, p, t, Mp, +1, s->partials, st);
         if (e == cudaSuccess) e = finish_on(s, kAlpha, st);
@@ -290,6 +381,55 @@ cudaError_t cg(gbds_solver s, const void *gauge, int recon, void *x, void *r, vo
             e = read_scalars(s, st);
             if (e != cudaSuccess) break;
             if (!(s->hsc->rr > target_rr)) break;  // converged (or NaN: stop)
+            if (sizeof(T) == 4 && stagnated(s->hsc->rr, k, best, best_k)) break;
+        }
+    }
+    *iters = k;
+    return e;
+}
+
+// The 16-bit operator: out = in - kappa^2 D_eo D_oe in, FP16 links.
+cudaError_t apply_M_h(gbds_solver s, const void *in, void *tmp, void *out, int isign, double *partials, cudaStream_t st) {
+    const Geom &g = s->g;
+    const float k2 = (float)(s->prm.kappa * s->prm.kappa);
+    cudaError_t e = launch_gen_h16(s->fmt16, g, s->prm.inner_recon, s->gauge16, in, tmp, isign, 0, nullptr, 0.f, nullptr, st);
+    if (e != cudaSuccess) return e;
+    return launch_gen_h16(s->fmt16, g, s->prm.inner_recon, s->gauge16, tmp, out, isign, 1, in, -k2, partials, st);
+}
+
+template <int FMT>
+cudaError_t cg_h(gbds_solver s, double target_rr, int max_iter, int *iters, cudaStream_t st) {
+    const Geom &g = s->g;
+    const int nb = blocks(g);
+    cudaError_t e = cudaSuccess;
+    int k = 0;
+    double best = 1e300;
+    int best_k = 0;
+    while (k < max_iter) {
+        e = apply_M_h(s, s->p16, s->t16, s->Mp16, +1, s->partials, st);
+        if (e == cudaSuccess) e = finish_on(s, kAlpha, st);
+        if (e == cudaSuccess) e = apply_M_h(s, s->Mp16, s->t16, s->Ap16, -1, nullptr, st);
+        if (e == cudaSuccess) {
+            cg_update_h<FMT><<<nb, kThreads, 0, st>>>(static_cast<float4 *>(s->e32), static_cast<float4 *>(s->r32),
+                                                       static_cast<const char *>(s->p16), static_cast<const char *>(s->Ap16),
+                                                       s->sc, g.Vh, g.stride, s->partials);
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = finish_on(s, kBeta, st);
+        if (e == cudaSuccess) {
+            cg_xpay_h<FMT><<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->r32), static_cast<char *>(s->p16), s->sc,
+                                                     g.Vh, g.stride);
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e != cudaSuccess) break;
+        k++;
+        if (k % 4 == 0 || k == max_iter) {
+            e = read_scalars(s, st);
+            if (e != cudaSuccess) break;
+            if (!(s->hsc->rr > target_rr)) break;
+            if (stagnated(s->hsc->rr, k, best, best_k)) break;
         }
     }
     *iters = k;
@@ -314,7 +454,8 @@ cudaError_t zero(gbds_solver s, void *v, cudaStream_t st) {
 
 void release(gbds_solver s) {
     void *bufs[] = {s->gauge64, s->gauge32, s->b64, s->c64, s->x64, s->r64, s->p64, s->Ap64, s->Mp64, s->t64,
-                    s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32, s->partials, s->sc};
+                    s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32, s->p16, s->Ap16, s->Mp16, s->t16, s->gauge16,
+                    s->partials, s->sc};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (s->hsc) cudaFreeHost(s->hsc);
@@ -325,8 +466,8 @@ void release(gbds_solver s) {
 extern "C" int gbds_solver_create(gbds_solver *out, const int dims[4], const gbds_solver_params *p) {
     if (!out || !p) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL argument");
     *out = nullptr;
-    if (p->inner_prec != 64 && p->inner_prec != 32)
-        return set_error(GBDS_ERROR_INVALID_VALUE, "inner_prec must be 64 or 32");
+    if (p->inner_prec != 64 && p->inner_prec != 32 && p->inner_prec != 16 && p->inner_prec != 17)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "inner_prec must be 64, 32, 16 or 17");
     if (p->inner_recon != 18 && p->inner_recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "inner_recon must be 18 or 12");
     if (!(p->tol > 0) || p->max_iter <= 0 || !(p->kappa > 0))
         return set_error(GBDS_ERROR_INVALID_VALUE, "tol, max_iter and kappa must be positive");
@@ -348,6 +489,17 @@ extern "C" int gbds_solver_create(gbds_solver *out, const int dims[4], const gbd
         for (void **b : d32)
             if (e == cudaSuccess) e = cudaMalloc(b, f32);
         if (e == cudaSuccess) e = cudaMalloc(&s->gauge32, gauge_bytes(g, 32, p->inner_recon));
+    } else if (p->inner_prec == 16 || p->inner_prec == 17) {
+        s->fmt16 = p->inner_prec == 16 ? kFmtF16N : kFmtBF16;
+        const size_t f16 = (size_t)gen_spinor_bytes(s->fmt16) * g.stride;
+        void **d32[] = {&s->e32, &s->r32};
+        for (void **b : d32)
+            if (e == cudaSuccess) e = cudaMalloc(b, f32);
+        void **d16[] = {&s->p16, &s->Ap16, &s->Mp16, &s->t16};
+        for (void **b : d16)
+            if (e == cudaSuccess) e = cudaMalloc(b, f16);
+        if (e == cudaSuccess) e = cudaMalloc(&s->gauge32, gauge_bytes(g, 32, p->inner_recon));
+        if (e == cudaSuccess) e = cudaMalloc(&s->gauge16, gauge_bytes(g, 32, p->inner_recon) / 2);
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->gauge64, gauge_bytes(g, 64, 18));
     if (e == cudaSuccess) e = cudaMalloc(&s->partials, sizeof(double) * (size_t)blocks(g));
@@ -376,7 +528,7 @@ extern "C" int gbds_solver_set_gauge(gbds_solver s, const double *u_packed, void
         return set_error(GBDS_ERROR_INVALID_VALUE, "u_packed must be a 16-byte aligned device pointer");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = launch_pack_gauge(s->g, 64, 18, u_packed, nullptr, s->gauge64, st);
-    if (e == cudaSuccess && s->prm.inner_prec == 32) {
+    if (e == cudaSuccess && s->prm.inner_prec != 64) {
         const size_t n = (size_t)s->g.V * 72;
         float *tmp = nullptr;
         e = cudaMallocAsync(reinterpret_cast<void **>(&tmp), n * sizeof(float), st);
@@ -385,6 +537,8 @@ extern "C" int gbds_solver_set_gauge(gbds_solver s, const double *u_packed, void
             count_launch();
             e = cudaGetLastError();
             if (e == cudaSuccess) e = launch_pack_gauge(s->g, 32, s->prm.inner_recon, tmp, nullptr, s->gauge32, st);
+            if (e == cudaSuccess && s->gauge16)
+                e = convert_links_f16(s->gauge32, s->gauge16, gauge_bytes(s->g, 32, s->prm.inner_recon) / 4, st);
             cudaFreeAsync(tmp, st);
         }
     }
@@ -458,10 +612,22 @@ static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, g
         } else {
             // FP64 defect correction around FP32 CG; r64 starts as c.
             e = norm_into<double>(s, s->c64, s->r64, nullptr, kOuterRR, st);
+            const bool half = s->prm.inner_prec != 32;
             while (e == cudaSuccess && outer_rr > tol2 * c2 && total < s->prm.max_iter) {
                 const int nb = blocks(g);
-                demote_residual<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->r64), static_cast<float4 *>(s->r32),
-                                                         static_cast<float4 *>(s->p32), s->sc, g.Vh, g.stride);
+                if (!half) {
+                    demote_residual<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->r64),
+                                                             static_cast<float4 *>(s->r32), static_cast<float4 *>(s->p32),
+                                                             s->sc, g.Vh, g.stride);
+                } else if (s->fmt16 == kFmtF16N) {
+                    demote_residual_h<kFmtF16N><<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->r64),
+                                                                         static_cast<float4 *>(s->r32),
+                                                                         static_cast<char *>(s->p16), s->sc, g.Vh, g.stride);
+                } else {
+                    demote_residual_h<kFmtBF16><<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->r64),
+                                                                         static_cast<float4 *>(s->r32),
+                                                                         static_cast<char *>(s->p16), s->sc, g.Vh, g.stride);
+                }
                 count_launch();
                 e = cudaGetLastError();
                 if (e == cudaSuccess) e = zero<float>(s, s->e32, st);
@@ -472,8 +638,13 @@ static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, g
                 const double need = 0.5 * s->prm.tol * std::sqrt(c2 / outer_rr);
                 if (need > delta) delta = need;
                 int it = 0;
-                e = cg<float>(s, s->gauge32, s->prm.inner_recon, s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32,
-                              delta * delta, s->prm.max_iter - total, &it, st);
+                if (!half)
+                    e = cg<float>(s, s->gauge32, s->prm.inner_recon, s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32,
+                                  delta * delta, s->prm.max_iter - total, &it, st);
+                else if (s->fmt16 == kFmtF16N)
+                    e = cg_h<kFmtF16N>(s, delta * delta, s->prm.max_iter - total, &it, st);
+                else
+                    e = cg_h<kFmtBF16>(s, delta * delta, s->prm.max_iter - total, &it, st);
                 total += it;
                 out.cycles++;
                 if (e != cudaSuccess) break;

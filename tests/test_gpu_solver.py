@@ -39,20 +39,21 @@ def test_apply_M_matches_oracle(dagger):
     s.close()
 
 
-@pytest.mark.parametrize("inner_prec,inner_recon", [(64, 18), (32, 18), (32, 12)])
+@pytest.mark.parametrize("inner_prec,inner_recon", [(64, 18), (32, 18), (32, 12), (16, 12), (17, 12), (16, 18)])
 def test_solve_reaches_tolerance(inner_prec, inner_recon):
     import torch
     from sse_wilson_dslash_gb300.device import WilsonSolver
     dims = (8, 8, 8, 8)
     lol = O.layout_table(O.LAYOUT_CB2, dims)
     u, b = O.make_inputs(dims, 51, 52, kind="near_unit")
-    s = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=inner_prec, inner_recon=inner_recon)
+    s = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=inner_prec, inner_recon=inner_recon,
+                     inner_tol=1e-5 if inner_prec >= 32 else 1e-3)
     s.set_gauge(torch.from_numpy(u.ravel()).cuda())
     x = torch.zeros(b.size, dtype=torch.float64, device="cuda")
     st = s.solve(torch.from_numpy(b.ravel()).cuda(), x)
     assert st["converged"] == 1 and st["residual"] <= 1e-10, st
     assert st["iterations"] > 5
-    if inner_prec == 32:
+    if inner_prec != 64:
         assert st["cycles"] >= 2
     # independent check: |b - M x| / |b| with the oracle's Dslash
     xv = x.cpu().numpy()
@@ -71,11 +72,13 @@ def test_mixed_and_fp64_solutions_agree():
     u, b = O.make_inputs(dims, 61, 62, kind="near_unit")
     ut, bt = torch.from_numpy(u.ravel()).cuda(), torch.from_numpy(b.ravel()).cuda()
     xs = []
-    for prec in (64, 32):
-        s = WilsonSolver(dims, KAPPA, tol=1e-11, inner_prec=prec, inner_recon=12)
+    for prec in (64, 32, 16, 17):
+        s = WilsonSolver(dims, KAPPA, tol=1e-11, inner_prec=prec, inner_recon=12,
+                         inner_tol=1e-5 if prec >= 32 else 1e-3)
         s.set_gauge(ut)
         x = torch.zeros_like(bt)
         assert s.solve(bt, x)["converged"] == 1
         xs.append(x)
         s.close()
-    assert (xs[0] - xs[1]).norm() / xs[0].norm() < 1e-9
+    for x in xs[1:]:
+        assert (xs[0] - x).norm() / xs[0].norm() < 1e-9
