@@ -9,8 +9,6 @@
 // (lib/shift_tables_scalar.c:240-263).
 #include <cuda_runtime.h>
 
-#include <algorithm>
-
 #include "gbds_internal.h"
 
 namespace gbds {
@@ -95,28 +93,20 @@ inline unsigned blocks_for(long long n, int threads) { return (unsigned)((n + th
 
 constexpr int kSpinorTile = 128;  // sites per block
 constexpr int kGaugeTile = 32;
-// Grid of the range kernels that move data over the host link: enough
-// blocks to keep ~200-400 GB/s of host traffic in flight, few enough to leave
-// most SMs to the Dslash and to the opposite-direction copies running beside
-// them.
-constexpr unsigned kHostGrid = 256;
 
 // packed: first site of checkerboard `parity` (sites [0, Vh) of that half).
 template <int UNITS>
 __global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int Vh, int stride, uint4 *__restrict__ soa,
                                                         int hb = 0) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
-    // grid-stride over tiles: a capped grid leaves SMs free for concurrent work
-    for (int h0 = hb + blockIdx.x * kSpinorTile; h0 < Vh; h0 += gridDim.x * kSpinorTile) {
-        const int n = min(kSpinorTile, Vh - h0);
-        const uint4 *src = packed + (size_t)h0 * UNITS;
-        for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) sm[e] = src[e];
-        __syncthreads();
-        for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
-            const int k = e / n, t = e - k * n;
-            soa[(size_t)k * stride + h0 + t] = sm[t * UNITS + k];
-        }
-        __syncthreads();
+    const int h0 = hb + blockIdx.x * kSpinorTile;
+    const int n = min(kSpinorTile, Vh - h0);
+    const uint4 *src = packed + (size_t)h0 * UNITS;
+    for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) sm[e] = src[e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
+        const int k = e / n, t = e - k * n;
+        soa[(size_t)k * stride + h0 + t] = sm[t * UNITS + k];
     }
 }
 
@@ -124,17 +114,15 @@ template <int UNITS>
 __global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restrict__ soa, int Vh, int stride, uint4 *packed,
                                                           int hb = 0) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
-    for (int h0 = hb + blockIdx.x * kSpinorTile; h0 < Vh; h0 += gridDim.x * kSpinorTile) {
-        const int n = min(kSpinorTile, Vh - h0);
-        for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
-            const int k = e / n, t = e - k * n;
-            sm[t * UNITS + k] = __ldg(soa + (size_t)k * stride + h0 + t);
-        }
-        __syncthreads();
-        uint4 *dst = packed + (size_t)h0 * UNITS;
-        for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) dst[e] = sm[e];
-        __syncthreads();
+    const int h0 = hb + blockIdx.x * kSpinorTile;
+    const int n = min(kSpinorTile, Vh - h0);
+    for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
+        const int k = e / n, t = e - k * n;
+        sm[t * UNITS + k] = __ldg(soa + (size_t)k * stride + h0 + t);
     }
+    __syncthreads();
+    uint4 *dst = packed + (size_t)h0 * UNITS;
+    for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) dst[e] = sm[e];
 }
 
 // Gauge: block of kGaugeTile consecutive caller sites (canonical order, both
@@ -146,42 +134,36 @@ __global__ void __launch_bounds__(128) pack_gauge_tile(const unsigned long long 
     constexpr int SITE_UNITS = 4 * 18 * sizeof(T) / 8;  // 8-byte units per site (4 links)
     constexpr int LINK_UNITS = 18 * sizeof(T) / 8;
     __shared__ unsigned long long sm[kGaugeTile * SITE_UNITS];
-    const int iend = ie < 0 ? g.V : ie;
+    const int i0 = ib + blockIdx.x * kGaugeTile;
+    const int n = min(kGaugeTile, (ie < 0 ? g.V : ie) - i0);
     const int used = g.nd * LINK_UNITS;  // leading units of each site that are read
+    const unsigned long long *src = packed + (size_t)i0 * SITE_UNITS;
+    for (int e = threadIdx.x; e < n * used; e += blockDim.x) {
+        const int t = e / used, u = e - t * used;
+        sm[t * SITE_UNITS + u] = src[(size_t)t * SITE_UNITS + u];
+    }
+    __syncthreads();
+    const T *st = reinterpret_cast<const T *>(sm);
     constexpr int C = sizeof(T) == 4 ? (RECON == 18 ? 9 : 3) : (RECON == 18 ? 9 : 6);
-    // grid-stride over tiles: a capped grid leaves SMs free for concurrent work
-    for (int i0 = ib + blockIdx.x * kGaugeTile; i0 < iend; i0 += gridDim.x * kGaugeTile) {
-        const int n = min(kGaugeTile, iend - i0);
-        const unsigned long long *src = packed + (size_t)i0 * SITE_UNITS;
-        for (int e = threadIdx.x; e < n * used; e += blockDim.x) {
-            const int t = e / used, u = e - t * used;
-            sm[t * SITE_UNITS + u] = src[(size_t)t * SITE_UNITS + u];
+    for (int e = threadIdx.x; e < n * g.nd * C; e += blockDim.x) {
+        const int t = e % n, rest = e / n;
+        const int mu = rest / C, k = rest % C;
+        const int i = i0 + t;
+        const int p = i >= g.Vh ? 1 : 0, h = i - p * g.Vh;
+        const T *m = st + (size_t)t * 72 + mu * 18;  // m[(3j+i)*2] = U_ij
+        char *blk = gauge + (size_t)(p * g.nd + mu) * block_bytes;
+        if constexpr (sizeof(T) == 4 && RECON == 18) {
+            const int r = k / 3, c = k % 3;
+            reinterpret_cast<float2 *>(blk)[(size_t)k * g.stride + h] = make_float2(m[(3 * c + r) * 2], m[(3 * c + r) * 2 + 1]);
+        } else if constexpr (sizeof(T) == 4) {
+            const int a = 2 * k, b = 2 * k + 1;  // complex components (row-major over rows 0, 1)
+            reinterpret_cast<float4 *>(blk)[(size_t)k * g.stride + h] =
+                make_float4(m[(3 * (a % 3) + a / 3) * 2], m[(3 * (a % 3) + a / 3) * 2 + 1],
+                            m[(3 * (b % 3) + b / 3) * 2], m[(3 * (b % 3) + b / 3) * 2 + 1]);
+        } else {
+            const int r = k / 3, c = k % 3;
+            reinterpret_cast<double2 *>(blk)[(size_t)k * g.stride + h] = make_double2(m[(3 * c + r) * 2], m[(3 * c + r) * 2 + 1]);
         }
-        __syncthreads();
-        const T *st = reinterpret_cast<const T *>(sm);
-        for (int e = threadIdx.x; e < n * g.nd * C; e += blockDim.x) {
-            const int t = e % n, rest = e / n;
-            const int mu = rest / C, k = rest % C;
-            const int i = i0 + t;
-            const int p = i >= g.Vh ? 1 : 0, h = i - p * g.Vh;
-            const T *m = st + (size_t)t * 72 + mu * 18;  // m[(3j+i)*2] = U_ij
-            char *blk = gauge + (size_t)(p * g.nd + mu) * block_bytes;
-            if constexpr (sizeof(T) == 4 && RECON == 18) {
-                const int r = k / 3, c = k % 3;
-                reinterpret_cast<float2 *>(blk)[(size_t)k * g.stride + h] =
-                    make_float2(m[(3 * c + r) * 2], m[(3 * c + r) * 2 + 1]);
-            } else if constexpr (sizeof(T) == 4) {
-                const int a = 2 * k, b = 2 * k + 1;  // complex components (row-major over rows 0, 1)
-                reinterpret_cast<float4 *>(blk)[(size_t)k * g.stride + h] =
-                    make_float4(m[(3 * (a % 3) + a / 3) * 2], m[(3 * (a % 3) + a / 3) * 2 + 1],
-                                m[(3 * (b % 3) + b / 3) * 2], m[(3 * (b % 3) + b / 3) * 2 + 1]);
-            } else {
-                const int r = k / 3, c = k % 3;
-                reinterpret_cast<double2 *>(blk)[(size_t)k * g.stride + h] =
-                    make_double2(m[(3 * c + r) * 2], m[(3 * c + r) * 2 + 1]);
-            }
-        }
-        __syncthreads();
     }
 }
 
@@ -269,7 +251,7 @@ cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_
 cudaError_t launch_pack_spinor_range(const Geom &g, int prec, const void *psi_packed, int parity, int h0, int h1,
                                      void *spinor, cudaStream_t stream) {
     if (h1 <= h0) return cudaSuccess;
-    const unsigned nb = std::min(blocks_for(h1 - h0, kSpinorTile), kHostGrid);
+    const unsigned nb = blocks_for(h1 - h0, kSpinorTile);
     const uint4 *src = static_cast<const uint4 *>(psi_packed) + (size_t)parity * g.Vh * (prec == 32 ? 6 : 12);
     if (prec == 32) pack_spinor_tile<6><<<nb, 128, 0, stream>>>(src, h1, g.stride, static_cast<uint4 *>(spinor), h0);
     else pack_spinor_tile<12><<<nb, 128, 0, stream>>>(src, h1, g.stride, static_cast<uint4 *>(spinor), h0);
@@ -280,7 +262,7 @@ cudaError_t launch_pack_spinor_range(const Geom &g, int prec, const void *psi_pa
 cudaError_t launch_unpack_spinor_range(const Geom &g, int prec, const void *spinor, int parity, int h0, int h1,
                                        void *psi_packed, cudaStream_t stream) {
     if (h1 <= h0) return cudaSuccess;
-    const unsigned nb = std::min(blocks_for(h1 - h0, kSpinorTile), kHostGrid);
+    const unsigned nb = blocks_for(h1 - h0, kSpinorTile);
     uint4 *dst = static_cast<uint4 *>(psi_packed) + (size_t)parity * g.Vh * (prec == 32 ? 6 : 12);
     if (prec == 32) unpack_spinor_tile<6><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), h1, g.stride, dst, h0);
     else unpack_spinor_tile<12><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), h1, g.stride, dst, h0);
@@ -294,7 +276,7 @@ cudaError_t launch_pack_gauge_range(const Geom &g, int prec, int recon, const vo
     const size_t bb = gauge_block_bytes(g, prec, recon);
     char *dst = static_cast<char *>(gauge);
     const unsigned long long *src = static_cast<const unsigned long long *>(u_packed);
-    const unsigned nt = std::min(blocks_for(i1 - i0, kGaugeTile), kHostGrid);
+    const unsigned nt = blocks_for(i1 - i0, kGaugeTile);
     if (prec == 32) {
         if (recon == 18) pack_gauge_tile<float, 18><<<nt, 128, 0, stream>>>(src, g, dst, bb, i0, i1);
         else pack_gauge_tile<float, 12><<<nt, 128, 0, stream>>>(src, g, dst, bb, i0, i1);
