@@ -552,27 +552,14 @@ def run_gb300(args):
         barrier()
         dt = time.perf_counter() - t0
         from sse_wilson_dslash_gb300 import legacy
-        path = {2: "direct, pipelined over 8 time-slabs (kernels read/write the pinned host arrays over "
-                   "NVLink-C2C; reads of slab k+1 overlap the write-back of slab k-1)",
-                1: "direct (kernels read/write the pinned host arrays over NVLink-C2C)",
-                0: "staged (cudaMemcpyAsync)"}[legacy.last_path()]
+        path = "direct (kernels read/write the pinned host arrays over NVLink-C2C)" if legacy.last_path() == 1 \
+            else "staged (cudaMemcpyAsync)"
         e2e = {"value": FLOPS_4D * sites * e2e_steps * world / dt / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": op.volume * 72 * 4 + sites * 96, "d2h_bytes_per_step": sites * 96,
                "steps": e2e_steps, "ms_per_step": dt / e2e_steps * 1e3,
                "path": "sse_su3dslash_wilson (libgbdslash32.so), pinned host arrays, gauge read every call, "
                        + path}
-        # the same calls without the slab pipeline, and staged through
-        # cudaMemcpyAsync, for comparison
-        legacy.set_pipeline(False)
-        d.sse_su3dslash_wilson(u_h, psi_h, res_h, 1, 0)
-        t0 = time.perf_counter()
-        for k in range(e2e_steps):
-            isign, cb = combos[k % 4]
-            d.sse_su3dslash_wilson(u_h, psi_h, res_h, isign, cb)
-        dt_1 = time.perf_counter() - t0
-        legacy.set_pipeline(True)
-        e2e["direct_one_pass"] = {"value": FLOPS_4D * sites * e2e_steps * world / dt_1 / 1e9,
-                                  "ms_per_step": dt_1 / e2e_steps * 1e3}
+        # the same calls staged through cudaMemcpyAsync, for comparison
         legacy.set_host_access(1)
         d.sse_su3dslash_wilson(u_h, psi_h, res_h, 1, 0)
         t0 = time.perf_counter()

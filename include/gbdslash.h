@@ -369,13 +369,8 @@ int gbds_legacy_set_recon(int recon);
  *               otherwise as 1;
  * 1           - stage every array through cudaMemcpyAsync. */
 int gbds_legacy_set_host_access(int mode);
-/* Path taken by the last legacy apply: 2 direct and pipelined over slabs of
- * the lattice (reads of slab k+1, the Dslash of slab k and the write-back of
- * slab k-1 overlap; lattices of >= 65536 sites with >= 4 planes in the
- * slowest direction), 1 direct, 0 staged, -1 none yet. */
+/* Path taken by the last legacy apply: 1 direct, 0 staged, -1 none yet. */
 int gbds_legacy_last_path(void);
-/* 1 (default): use the slab pipeline where it applies; 0: one pass. */
-int gbds_legacy_set_pipeline(int on);
 
 /* Refcount of a legacy context: prec 32/64, nd 4/3 (0 = not initialised). */
 int gbds_legacy_refcount(int prec, int nd);

@@ -83,7 +83,7 @@ def core() -> ctypes.CDLL:
     L.gbds_op_unpack_spinor.argtypes = [vp, vp, i, vp, vp]
     L.gbds_op_dslash.argtypes = [vp, vp, vp, vp, i, i, vp]
     for n in ("gbds_legacy_set_exit_on_error", "gbds_legacy_set_gauge_cache", "gbds_legacy_set_recon",
-              "gbds_legacy_set_host_access", "gbds_legacy_set_pipeline"):
+              "gbds_legacy_set_host_access"):
         getattr(L, n).argtypes = [i]
     L.gbds_legacy_refcount.argtypes = [i, i]
     L.gbds_layout_select.argtypes = [i, c_int_p]

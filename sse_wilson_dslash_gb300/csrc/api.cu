@@ -329,8 +329,6 @@ struct LegacyCtx {
     gbds_op op = nullptr;
     bool canonical = true;
     cudaStream_t stream = nullptr;
-    cudaStream_t load_stream = nullptr;  // slab pipeline: host reads run here
-    cudaEvent_t slab_loaded[8] = {};
     void *d_u_packed = nullptr;    // V*4*18 reals
     void *d_gauge = nullptr;       // internal layout
     void *d_psi_packed = nullptr;  // canonical: Vh*24 reals, else V*24
@@ -345,8 +343,7 @@ int g_exit_on_error = 1;
 int g_gauge_cache = 0;
 int g_legacy_recon = 18;
 int g_host_access = 0;  // 0: read/write host arrays directly where the GPU can; 1: always stage
-int g_last_path = -1;   // 0 staged, 1 direct, 2 direct pipelined over slabs
-int g_pipeline = 1;     // pipeline the direct path over slabs (large lattices)
+int g_last_path = -1;   // 0 staged, 1 direct
 
 // Address under which kernels can use a caller array, or nullptr when the
 // GPU cannot reach it directly.  Pinned / registered host memory has a device
@@ -376,13 +373,9 @@ LegacyCtx &ctx_for(int prec, int nd) { return g_legacy[prec == 32 ? 0 : 1][nd ==
 
 void legacy_release(LegacyCtx &c) {
     if (c.stream) cudaStreamSynchronize(c.stream);
-    if (c.load_stream) cudaStreamSynchronize(c.load_stream);
     void *bufs[] = {c.d_u_packed, c.d_gauge, c.d_psi_packed, c.d_res_packed, c.d_psi, c.d_res};
     for (void *b : bufs)
         if (b) cudaFree(b);
-    for (cudaEvent_t ev : c.slab_loaded)
-        if (ev) cudaEventDestroy(ev);
-    if (c.load_stream) cudaStreamDestroy(c.load_stream);
     if (c.stream) cudaStreamDestroy(c.stream);
     gbds_op_destroy(c.op);
     c = LegacyCtx();
@@ -461,8 +454,6 @@ void legacy_init(int prec, int nd, const int *latt_size, void (*getSiteCoords)(i
     const size_t real = prec == 32 ? 4 : 8;
     const size_t spin_sites = canonical ? (size_t)g.Vh : (size_t)g.V;
     cudaError_t e = cudaStreamCreateWithFlags(&n.stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&n.load_stream, cudaStreamNonBlocking);
-    for (int k = 0; k < 8 && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&n.slab_loaded[k], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&n.d_u_packed, (size_t)g.V * 4 * 18 * real);
     if (e == cudaSuccess) e = cudaMalloc(&n.d_gauge, gbds_op_gauge_bytes(n.op));
     if (e == cudaSuccess) e = cudaMalloc(&n.d_psi_packed, spin_sites * 24 * real);
@@ -484,53 +475,6 @@ void legacy_free(int prec, int nd) {
     LegacyCtx &c = ctx_for(prec, nd);
     if (c.refcount == 0) return;
     if (--c.refcount == 0) legacy_release(c);
-}
-
-// Direct path, pipelined over slabs of the slowest coordinate of the site
-// order (t in 4D, z in 3D): slab k+1 is read from the host while slab k is
-// computed and the result of slab k-1 is written back, so host reads and
-// writes overlap.  Output slab k needs input slabs k-1, k, k+1 (periodic):
-// reads go in the order n-1, 0, 1, ..., n-2 and slab k is computed once
-// slabs k-1, k, k+1 are in.
-cudaError_t legacy_pipelined(LegacyCtx &c, int prec, const void *du, bool load_gauge, const void *dpsi, void *dres,
-                             int isign, int cb) {
-    const Geom &g = c.op->g;
-    const int Ls = g.nd == 4 ? g.L[3] : g.L[2];
-    const int plane = g.Vh / Ls;
-    const int ns = Ls < 8 ? Ls : 8;
-    const int target = 1 - cb;
-    cudaStream_t L = c.load_stream, C = c.stream;
-    auto range = [&](int k, int &h0, int &h1) {
-        h0 = (int)((long long)k * Ls / ns) * plane;
-        h1 = (int)((long long)(k + 1) * Ls / ns) * plane;
-    };
-    cudaError_t e = cudaSuccess;
-    for (int j = 0; j < ns && e == cudaSuccess; j++) {
-        const int k = (j + ns - 1) % ns;  // n-1, 0, 1, ..., n-2
-        int h0, h1;
-        range(k, h0, h1);
-        if (load_gauge) {
-            e = launch_pack_gauge_range(g, prec, c.op->recon, du, h0, h1, c.d_gauge, L);
-            if (e == cudaSuccess) e = launch_pack_gauge_range(g, prec, c.op->recon, du, g.Vh + h0, g.Vh + h1, c.d_gauge, L);
-        }
-        if (e == cudaSuccess) e = launch_pack_spinor_range(g, prec, dpsi, cb, h0, h1, c.d_psi, L);
-        if (e == cudaSuccess) e = cudaEventRecord(c.slab_loaded[k], L);
-    }
-    for (int k = 0; k < ns && e == cudaSuccess; k++) {
-        const int need[3] = {(k + ns - 1) % ns, k, (k + 1) % ns};
-        for (int q = 0; q < 3 && e == cudaSuccess; q++) e = cudaStreamWaitEvent(C, c.slab_loaded[need[q]], 0);
-        int h0, h1;
-        range(k, h0, h1);
-        if (e == cudaSuccess)
-            e = prec == 32 ? launch_dslash_f32(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block,
-                                               c.op->variant, C, h0, h1)
-                           : launch_dslash_f64(g, c.op->recon, c.d_gauge, c.d_psi, c.d_res, isign, cb, c.op->block,
-                                               c.op->variant, C, h0, h1);
-        if (e == cudaSuccess) e = launch_unpack_spinor_range(g, prec, c.d_res, target, h0, h1, dres, C);
-    }
-    cudaError_t e2 = cudaStreamSynchronize(L);
-    cudaError_t e3 = cudaStreamSynchronize(C);
-    return e != cudaSuccess ? e : (e2 != cudaSuccess ? e2 : e3);
 }
 
 void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, int isign, int cb, const char *fn) {
@@ -565,14 +509,6 @@ void legacy_apply(int prec, int nd, const void *u, const void *psi, void *res, i
     }
     const bool aligned = ((reinterpret_cast<uintptr_t>(du) | reinterpret_cast<uintptr_t>(dpsi) |
                            reinterpret_cast<uintptr_t>(dres)) & 15u) == 0;
-    const int Ls = g.nd == 4 ? g.L[3] : g.L[2];
-    if (du && dpsi && dres && aligned && g_pipeline && Ls >= 4 && g.V >= (1 << 16)) {
-        e = legacy_pipelined(c, prec, du, !reuse_gauge, dpsi, dres, isign, cb);
-        c.cached_u = e == cudaSuccess ? u : nullptr;
-        g_last_path = 2;
-        if (e != cudaSuccess) fprintf(stderr, "%s: CUDA error: %s\n", fn, cudaGetErrorString(e));
-        return;
-    }
     if (du && dpsi && dres && aligned) {
         // Direct: the layout kernels read u and psi and write res where they
         // lie, with no intermediate copy.
@@ -712,11 +648,6 @@ extern "C" int gbds_legacy_set_host_access(int mode) {
 }
 
 extern "C" int gbds_legacy_last_path(void) { return g_last_path; }
-
-extern "C" int gbds_legacy_set_pipeline(int on) {
-    g_pipeline = on ? 1 : 0;
-    return GBDS_SUCCESS;
-}
 
 extern "C" int gbds_legacy_refcount(int prec, int nd) {
     if ((prec != 32 && prec != 64) || (nd != 3 && nd != 4)) return -1;

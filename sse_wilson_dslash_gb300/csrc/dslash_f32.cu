@@ -3,8 +3,8 @@
 
 namespace gbds {
 cudaError_t launch_dslash_f32(const Geom &g, int recon, const void *gauge, const void *psi, void *res,
-                              int isign, int cb, int block, int variant, cudaStream_t stream, int h_begin, int h_end) {
-    return launch_dslash_t<float>(g, recon, gauge, psi, res, isign, cb, block, variant, stream, h_begin, h_end);
+                              int isign, int cb, int block, int variant, cudaStream_t stream) {
+    return launch_dslash_t<float>(g, recon, gauge, psi, res, isign, cb, block, variant, stream);
 }
 int dslash_variants(int prec) { return prec == 32 ? Variants<float>::n : Variants<double>::n; }
 cudaError_t launch_dslash_xpay_f32(const Geom &g, int recon, const void *gauge, const void *psi, const void *x,

@@ -272,7 +272,6 @@ struct DslashArgs {
     const char *gauge;                // both checkerboards
     size_t link_block_bytes;          // bytes of one (parity, mu) block
     int pt;                           // target parity = 1 - cb
-    int h_begin, h_end;               // target sites [h_begin, h_end) of this launch
 };
 
 template <typename T, int ND, int RECON, int ISIGN, int MU>
@@ -301,8 +300,8 @@ template <> struct Bounds<0> { static constexpr int threads = 256, blocks = 1; }
 
 template <typename T, int ND, int RECON, int ISIGN, int MINB>
 __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks) dslash_kernel(const DslashArgs<T> a) {
-    const int h = a.h_begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= a.h_end) return;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= a.g.Vh) return;
     Nbr n;
     neighbours<ND>(a.g, h, a.pt, n);
     cx<T> acc[4][3];
@@ -415,8 +414,6 @@ cudaError_t launch_dslash_xpay_t(const Geom &g, int recon, const void *gauge, co
     const int vec_bytes = sizeof(T) == 4 ? (recon == 18 ? 8 : 16) : 16;
     a.link_block_bytes = (size_t)Field<T>::link_vecs(recon) * g.stride * vec_bytes;
     a.pt = 1 - cb;
-    a.h_begin = 0;
-    a.h_end = g.Vh;
     const dim3 grid(xpay_blocks(g));
     const auto *xv = static_cast<const typename VecOf<T>::S *>(x);
     constexpr int m18 = XpayMinb<T>::r18, m12 = XpayMinb<T>::r12;
@@ -456,8 +453,7 @@ inline void launch_minb<double>(const DslashArgs<double> &a, dim3 grid, int bloc
 
 template <typename T>
 cudaError_t launch_dslash_t(const Geom &g, int recon, const void *gauge, const void *psi, void *res,
-                            int isign, int cb, int block, int variant, cudaStream_t stream, int h_begin = 0,
-                            int h_end = -1) {
+                            int isign, int cb, int block, int variant, cudaStream_t stream) {
     DslashArgs<T> a;
     a.g = g;
     a.psi = static_cast<const typename VecOf<T>::S *>(psi);
@@ -466,13 +462,10 @@ cudaError_t launch_dslash_t(const Geom &g, int recon, const void *gauge, const v
     const int vec_bytes = sizeof(T) == 4 ? (recon == 18 ? 8 : 16) : 16;
     a.link_block_bytes = (size_t)Field<T>::link_vecs(recon) * g.stride * vec_bytes;
     a.pt = 1 - cb;
-    a.h_begin = h_begin;
-    a.h_end = h_end < 0 ? g.Vh : h_end;
-    if (a.h_end <= a.h_begin) return cudaSuccess;
     if (variant < 0 || variant >= Variants<T>::n) variant = 0;
     if (block <= 0) block = 128;
     if (Variants<T>::minb[variant] > 0) block = 128;  // the register cap assumes 128-thread blocks
-    const dim3 grid((a.h_end - a.h_begin + block - 1) / block);
+    const dim3 grid((g.Vh + block - 1) / block);
     switch (Variants<T>::minb[variant]) {
     case 0: launch_variant<T, 0>(a, grid, block, g.nd, recon, isign, stream); break;
     default: launch_minb<T>(a, grid, block, g.nd, recon, isign, Variants<T>::minb[variant], stream); break;

@@ -30,13 +30,10 @@ void count_launch(int n = 1);
 // All pointers are device pointers; `stream` is a cudaStream_t.
 // block: threads per block (0 = default); variant: register-cap variant
 // (0 = uncapped; see Variants<T> in dslash_kernel.cuh).
-// [h_begin, h_end): target sites of this launch (default: all).
 cudaError_t launch_dslash_f32(const Geom &g, int recon, const void *gauge, const void *psi,
-                              void *res, int isign, int cb, int block, int variant, cudaStream_t stream,
-                              int h_begin = 0, int h_end = -1);
+                              void *res, int isign, int cb, int block, int variant, cudaStream_t stream);
 cudaError_t launch_dslash_f64(const Geom &g, int recon, const void *gauge, const void *psi,
-                              void *res, int isign, int cb, int block, int variant, cudaStream_t stream,
-                              int h_begin = 0, int h_end = -1);
+                              void *res, int isign, int cb, int block, int variant, cudaStream_t stream);
 int dslash_variants(int prec);
 
 // res = x + coef * Dslash(psi) (4D; res and x on checkerboard 1-cb); if
@@ -79,16 +76,6 @@ inline int gen_spinor_bytes(int fmt) { return fmt == 0 ? 96 : (fmt == 1 ? 48 : 5
 cudaError_t launch_gen_h16(int fmt, const Geom &g, int recon, const void *gauge, const void *psi, void *res, int isign,
                            int cb, const void *x, float coef, double *partials, cudaStream_t st);
 cudaError_t convert_links_f16(const void *gauge32, void *gauge16, size_t nfloats, cudaStream_t st);
-
-// Canonical-layout layout kernels over a sub-range, for pipelining:
-// spinors: sites [h0, h1) of checkerboard `parity`, packed array = full lattice;
-// gauge: caller sites [i0, i1) (both checkerboards are in the caller order).
-cudaError_t launch_pack_spinor_range(const Geom &g, int prec, const void *psi_packed, int parity, int h0, int h1,
-                                     void *spinor, cudaStream_t stream);
-cudaError_t launch_unpack_spinor_range(const Geom &g, int prec, const void *spinor, int parity, int h0, int h1,
-                                       void *psi_packed, cudaStream_t stream);
-cudaError_t launch_pack_gauge_range(const Geom &g, int prec, int recon, const void *u_packed, int i0, int i1, void *gauge,
-                                    cudaStream_t stream);
 
 // Sizes in bytes of the internal fields.
 size_t spinor_bytes(const Geom &g, int prec);

@@ -96,10 +96,9 @@ constexpr int kGaugeTile = 32;
 
 // packed: first site of checkerboard `parity` (sites [0, Vh) of that half).
 template <int UNITS>
-__global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int Vh, int stride, uint4 *__restrict__ soa,
-                                                        int hb = 0) {
+__global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int Vh, int stride, uint4 *__restrict__ soa) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
-    const int h0 = hb + blockIdx.x * kSpinorTile;
+    const int h0 = blockIdx.x * kSpinorTile;
     const int n = min(kSpinorTile, Vh - h0);
     const uint4 *src = packed + (size_t)h0 * UNITS;
     for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) sm[e] = src[e];
@@ -111,10 +110,9 @@ __global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int
 }
 
 template <int UNITS>
-__global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restrict__ soa, int Vh, int stride, uint4 *packed,
-                                                          int hb = 0) {
+__global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restrict__ soa, int Vh, int stride, uint4 *packed) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
-    const int h0 = hb + blockIdx.x * kSpinorTile;
+    const int h0 = blockIdx.x * kSpinorTile;
     const int n = min(kSpinorTile, Vh - h0);
     for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
         const int k = e / n, t = e - k * n;
@@ -130,12 +128,12 @@ __global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restric
 // bytes (one float2 / one double) keep the 3D skip of mu = 3 exact.
 template <typename T, int RECON>
 __global__ void __launch_bounds__(128) pack_gauge_tile(const unsigned long long *packed, Geom g, char *__restrict__ gauge,
-                                                        size_t block_bytes, int ib = 0, int ie = -1) {
+                                                        size_t block_bytes) {
     constexpr int SITE_UNITS = 4 * 18 * sizeof(T) / 8;  // 8-byte units per site (4 links)
     constexpr int LINK_UNITS = 18 * sizeof(T) / 8;
     __shared__ unsigned long long sm[kGaugeTile * SITE_UNITS];
-    const int i0 = ib + blockIdx.x * kGaugeTile;
-    const int n = min(kGaugeTile, (ie < 0 ? g.V : ie) - i0);
+    const int i0 = blockIdx.x * kGaugeTile;
+    const int n = min(kGaugeTile, g.V - i0);
     const int used = g.nd * LINK_UNITS;  // leading units of each site that are read
     const unsigned long long *src = packed + (size_t)i0 * SITE_UNITS;
     for (int e = threadIdx.x; e < n * used; e += blockDim.x) {
@@ -243,46 +241,6 @@ cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_
         const double *src = static_cast<const double *>(u_packed);
         if (recon == 18) pack_gauge_kernel<double, 18><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb);
         else pack_gauge_kernel<double, 12><<<nb, 128, 0, stream>>>(src, site_table, g, dst, bb);
-    }
-    count_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_pack_spinor_range(const Geom &g, int prec, const void *psi_packed, int parity, int h0, int h1,
-                                     void *spinor, cudaStream_t stream) {
-    if (h1 <= h0) return cudaSuccess;
-    const unsigned nb = blocks_for(h1 - h0, kSpinorTile);
-    const uint4 *src = static_cast<const uint4 *>(psi_packed) + (size_t)parity * g.Vh * (prec == 32 ? 6 : 12);
-    if (prec == 32) pack_spinor_tile<6><<<nb, 128, 0, stream>>>(src, h1, g.stride, static_cast<uint4 *>(spinor), h0);
-    else pack_spinor_tile<12><<<nb, 128, 0, stream>>>(src, h1, g.stride, static_cast<uint4 *>(spinor), h0);
-    count_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_unpack_spinor_range(const Geom &g, int prec, const void *spinor, int parity, int h0, int h1,
-                                       void *psi_packed, cudaStream_t stream) {
-    if (h1 <= h0) return cudaSuccess;
-    const unsigned nb = blocks_for(h1 - h0, kSpinorTile);
-    uint4 *dst = static_cast<uint4 *>(psi_packed) + (size_t)parity * g.Vh * (prec == 32 ? 6 : 12);
-    if (prec == 32) unpack_spinor_tile<6><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), h1, g.stride, dst, h0);
-    else unpack_spinor_tile<12><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), h1, g.stride, dst, h0);
-    count_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_pack_gauge_range(const Geom &g, int prec, int recon, const void *u_packed, int i0, int i1, void *gauge,
-                                    cudaStream_t stream) {
-    if (i1 <= i0) return cudaSuccess;
-    const size_t bb = gauge_block_bytes(g, prec, recon);
-    char *dst = static_cast<char *>(gauge);
-    const unsigned long long *src = static_cast<const unsigned long long *>(u_packed);
-    const unsigned nt = blocks_for(i1 - i0, kGaugeTile);
-    if (prec == 32) {
-        if (recon == 18) pack_gauge_tile<float, 18><<<nt, 128, 0, stream>>>(src, g, dst, bb, i0, i1);
-        else pack_gauge_tile<float, 12><<<nt, 128, 0, stream>>>(src, g, dst, bb, i0, i1);
-    } else {
-        if (recon == 18) pack_gauge_tile<double, 18><<<nt, 128, 0, stream>>>(src, g, dst, bb, i0, i1);
-        else pack_gauge_tile<double, 12><<<nt, 128, 0, stream>>>(src, g, dst, bb, i0, i1);
     }
     count_launch();
     return cudaGetLastError();

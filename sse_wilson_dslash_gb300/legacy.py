@@ -112,13 +112,8 @@ def set_host_access(mode: int) -> None:
     _lib.check(_lib.core().gbds_legacy_set_host_access(int(mode)))
 
 
-def set_pipeline(on: bool) -> None:
-    """Pipeline the direct path over slabs of the lattice (default on)."""
-    _lib.core().gbds_legacy_set_pipeline(1 if on else 0)
-
-
 def last_path() -> int:
-    """2 direct and pipelined, 1 direct, 0 staged copies."""
+    """1 if the last apply used direct host access, 0 if it staged copies."""
     return int(_lib.core().gbds_legacy_last_path())
 
 

@@ -169,44 +169,6 @@ def test_pinned_host_arrays_take_the_direct_path(dropin):
         _free(d, 4)
 
 
-@pytest.mark.parametrize("prec", [32, 64])
-@pytest.mark.parametrize("nd,dims", [(4, (16, 16, 16, 16)), (3, (16, 16, 32, 8)), (4, (8, 8, 32, 36))])
-def test_pipelined_direct_path(dropin, prec, nd, dims):
-    """Large lattices on pinned host arrays take the slab pipeline (reads of
-    slab k+1, the Dslash of slab k and the write-back of slab k-1 overlap);
-    every isign/cb against the oracle, and bit-identical to the one-pass path."""
-    import torch
-    from sse_wilson_dslash_gb300 import legacy
-    d = dropin[prec]
-    kind = O.LAYOUT_CB2 if nd == 4 else O.LAYOUT_CB3D
-    lol = O.layout_table(kind, dims)
-    _init(d, nd, dims, kind, None)
-    try:
-        u, psi = O.make_inputs(dims, 71, 72)
-        V = O.volume(dims)
-        dt = d.dtype
-        ut = torch.from_numpy(u.astype(dt).ravel()).pin_memory()
-        pt = torch.from_numpy(psi.astype(dt).ravel()).pin_memory()
-        for isign, cb in ((1, 0), (-1, 1), (-1, 0), (1, 1)):
-            rt = torch.full((V * 24,), 1.5, dtype=ut.dtype).pin_memory()
-            _apply(d, nd, ut, pt, rt, isign, cb)
-            assert legacy.last_path() == 2
-            res = rt.numpy().reshape(V, 4, 3, 2).copy()
-            other = O.target_sites(nd, dims, lol, 1 - cb)
-            assert np.all(res.reshape(V, 24)[other] == 1.5)
-            ref = O.dslash_plain(nd, dims, lol, u.astype(dt), psi.astype(dt), isign, cb)
-            assert O.site_rel_err(res, ref, O.target_sites(nd, dims, lol, cb)) <= SITE_TOL[prec]
-            legacy.set_pipeline(False)
-            r1 = torch.full((V * 24,), 1.5, dtype=ut.dtype).pin_memory()
-            _apply(d, nd, ut, pt, r1, isign, cb)
-            legacy.set_pipeline(True)
-            assert legacy.last_path() == 1
-            assert torch.equal(r1, rt)
-    finally:
-        legacy.set_pipeline(True)
-        _free(d, nd)
-
-
 def test_autotune_picks_a_valid_configuration_and_keeps_results():
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
