@@ -271,6 +271,32 @@ def multi_rhs_variants(torch, steps, peak):
             del gauge, srcs, outs
             op.close()
             torch.cuda.empty_cache()
+    # 16-bit storage with 16 / 32 right-hand sides: colour multiply on the
+    # CUDA cores ("cc") and on the tensor cores ("tc")
+    for fmt in ("bf16", "f16"):
+        for nrhs in (16, 32):
+            for tc in (False, True):
+                key = f"{fmt}_nrhs{nrhs}_{'tc' if tc else 'cc'}"
+                if not tc and fmt == "bf16":
+                    out[key] = out[f"bf16_nrhs{nrhs}"]
+                    continue
+                op = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
+                if tc:
+                    op.set_tensor_cores(True)
+                gauge = op.pack_gauge(u)
+                psi = torch.randn(nrhs * V * 24, dtype=torch.float32, device="cuda", generator=gen)
+                srcs = [op.pack_spinor(psi, 0), op.pack_spinor(psi, 1)]
+                del psi
+                outs = [op.new_spinor(), op.new_spinor()]
+                ms = time_device(op, gauge, srcs, outs, max(10, steps // max(1, nrhs // 4)), 3, torch)
+                op.check()
+                sites = op.volume_cb * nrhs
+                gbs = op.bytes_per_site * sites / (ms * 1e6)
+                out[key] = {"ms": ms, "gflops": 1320 * sites / (ms * 1e6), "gbs": gbs, "roofline_frac": gbs / peak,
+                            "ms_per_rhs": ms / nrhs, "bytes_per_site_rhs": op.bytes_per_site}
+                del gauge, srcs, outs
+                op.close()
+                torch.cuda.empty_cache()
     return out
 
 

@@ -102,6 +102,16 @@ int gbds_op_destroy(gbds_op op);
 int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int prec, int recon, int nrhs, int format);
 int gbds_op_nrhs(gbds_op op);
 
+/* 16-bit spinor formats with 16 or 32 right-hand sides: do the colour
+ * multiply of each hop on the tensor cores (tcgen05.mma, FP32 accumulation in
+ * TMEM) for all right-hand sides of a few sites at once; the links enter as
+ * bfloat16 (GBDS_SPINOR_BF16) or half (GBDS_SPINOR_F16_NORM) operands.
+ * Spin projection and reconstruction stay on the CUDA cores.  gbds_op_check
+ * synchronises and reports a tensor-core launch whose bounded wait for its
+ * MMAs ran out (it then wrote nothing for those sites). */
+int gbds_op_set_tensor_cores(gbds_op op, int on);
+int gbds_op_check(gbds_op op);
+
 /* Caller site layout for pack/unpack: site_table[i] = caller linear index of
  * internal site i (i = p*Vh + h, internal order above), n = V entries, a
  * permutation of [0, V).  NULL (or the identity) selects the canonical
@@ -195,7 +205,8 @@ int gbds_dslash_packed_noalloc_f32(const int dims[4], int nd, const float *u_pac
  * launch walks it with a fixed stride, so no CTA waits on another and the
  * launch can be captured in a CUDA graph (gbds_batch_capture_graph; later
  * gbds_batch_launch calls replay the graph).  Pointers are fixed at create
- * time. */
+ * time.  At most 32 lattices per batch (the descriptors travel in the kernel
+ * parameters). */
 typedef struct gbds_batch_item {
     int dims[4];
     int nrhs;

@@ -66,6 +66,8 @@ def core() -> ctypes.CDLL:
     L.gbds_op_create.argtypes = [ctypes.POINTER(vp), c_int_p, i, i, i]
     L.gbds_op_create_ex.argtypes = [ctypes.POINTER(vp), c_int_p, i, i, i, i, i]
     L.gbds_op_nrhs.argtypes = [vp]
+    L.gbds_op_set_tensor_cores.argtypes = [vp, i]
+    L.gbds_op_check.argtypes = [vp]
     L.gbds_op_destroy.argtypes = [vp]
     L.gbds_op_set_layout.argtypes = [vp, c_int_p, i]
     L.gbds_op_is_canonical.argtypes = [vp]

@@ -119,6 +119,8 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     o->variant = (prec == 32 && recon == 18) ? 1 : 0;
     o->nrhs = nrhs;
     o->format = format;
+    o->tensor_cores = 0;
+    o->d_err = nullptr;
     o->d_site_table = nullptr;
     *op = o;
     return GBDS_SUCCESS;
@@ -127,6 +129,7 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
 extern "C" int gbds_op_destroy(gbds_op op) {
     if (!op) return GBDS_SUCCESS;
     if (op->d_site_table) cudaFree(op->d_site_table);
+    if (op->d_err) cudaFree(op->d_err);
     delete op;
     return GBDS_SUCCESS;
 }
@@ -170,6 +173,32 @@ extern "C" size_t gbds_op_spinor_bytes(gbds_op op) {
 }
 
 extern "C" int gbds_op_nrhs(gbds_op op) { return op ? op->nrhs : 0; }
+
+extern "C" int gbds_op_set_tensor_cores(gbds_op op, int on) {
+    if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
+    if (on && (op->format == GBDS_SPINOR_NATIVE || (op->nrhs != 16 && op->nrhs != 32)))
+        return set_error(GBDS_ERROR_UNSUPPORTED, "tensor cores need a 16-bit spinor format and 16 or 32 right-hand sides");
+    if (on && !op->d_err) {
+        cudaError_t e = cudaMalloc(&op->d_err, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(op->d_err, 0, sizeof(int));
+        if (e != cudaSuccess) return cuda_error(e, "gbds_op_set_tensor_cores");
+    }
+    op->tensor_cores = on ? 1 : 0;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_op_check(gbds_op op) {
+    if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
+    if (!op->d_err) return GBDS_SUCCESS;
+    int v = 0;
+    cudaError_t e = cudaMemcpy(&v, op->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_op_check");
+    if (v) {
+        cudaMemset(op->d_err, 0, sizeof(int));
+        return set_error(GBDS_ERROR_CUDA, "a tensor-core Dslash launch timed out waiting for its MMAs");
+    }
+    return GBDS_SUCCESS;
+}
 
 extern "C" size_t gbds_op_gauge_bytes(gbds_op op) { return op ? gauge_bytes(op->g, op->prec, op->recon) : 0; }
 
@@ -306,6 +335,10 @@ extern "C" int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, vo
     if (!aligned16(gauge) || !aligned16(psi) || !aligned16(res))
         return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (generic(op) && op->tensor_cores) {
+        cudaError_t e = launch_gen_tc(op->format, op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, op->d_err, s);
+        return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash (tensor cores)");
+    }
     if (generic(op)) {
         cudaError_t e = op->format == GBDS_SPINOR_NATIVE
                             ? launch_gen_f32(op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f, nullptr, s)

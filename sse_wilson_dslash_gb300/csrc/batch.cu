@@ -36,25 +36,35 @@ struct Tile {
     int end;
 };
 
-template <int FMT, int RECON, int ISIGN, int MU>
+// Lattice descriptors travel by value in the kernel parameters (the constant
+// bank: one broadcast read per warp), not through global memory.
+constexpr int kMaxBatch = 32;
+struct BatchParams {
+    int n;
+    Problem p[kMaxBatch];
+};
+
+template <int FMT, int RECON, int ISIGN, int NRHS, int MU>
 __device__ __forceinline__ void batch_hop_pair(const Problem &P, int h, int r, const Nbr &n, cx<float> (&acc)[4][3]) {
     const int ps = 1 - P.pt;
+    const int nr = NRHS > 0 ? NRHS : P.nrhs;
     cx<float> s[4][3], hs[2][3], w[2][3], U[3][3];
-    Sio<FMT>::load(P.psi, P.cs, (size_t)n.f[MU] * P.nrhs + r, s);
+    Sio<FMT>::load(P.psi, P.cs, (size_t)n.f[MU] * nr + r, s);
     Field<float>::template load_link<RECON>(P.gauge + (size_t)(P.pt * 4 + MU) * P.link_block_bytes, P.g.stride, h, U);
     project<MU, ISIGN>(s, hs);
     su3_mul<false>(U, hs, w);
     reconstruct<MU, ISIGN>(acc, w);
-    Sio<FMT>::load(P.psi, P.cs, (size_t)n.b[MU] * P.nrhs + r, s);
+    Sio<FMT>::load(P.psi, P.cs, (size_t)n.b[MU] * nr + r, s);
     Field<float>::template load_link<RECON>(P.gauge + (size_t)(ps * 4 + MU) * P.link_block_bytes, P.g.stride, n.b[MU], U);
     project<MU, -ISIGN>(s, hs);
     su3_mul<true>(U, hs, w);
     reconstruct<MU, -ISIGN>(acc, w);
 }
 
-template <int FMT, int RECON, int ISIGN>
+template <int FMT, int RECON, int ISIGN, int NRHS>
 __device__ __forceinline__ void batch_site(const Problem &P, int t) {
-    const int h = t / P.nrhs, r = t - h * P.nrhs;
+    const int nr = NRHS > 0 ? NRHS : P.nrhs;
+    const int h = t / nr, r = t - h * nr;
     Nbr n;
     neighbours<4>(P.g, h, P.pt, n);
     cx<float> acc[4][3];
@@ -62,23 +72,26 @@ __device__ __forceinline__ void batch_site(const Problem &P, int t) {
     for (int s = 0; s < 4; s++)
 #pragma unroll
         for (int c = 0; c < 3; c++) acc[s][c] = {0.f, 0.f};
-    batch_hop_pair<FMT, RECON, ISIGN, 0>(P, h, r, n, acc);
-    batch_hop_pair<FMT, RECON, ISIGN, 1>(P, h, r, n, acc);
-    batch_hop_pair<FMT, RECON, ISIGN, 2>(P, h, r, n, acc);
-    batch_hop_pair<FMT, RECON, ISIGN, 3>(P, h, r, n, acc);
-    Sio<FMT>::store(P.res, P.cs, (size_t)h * P.nrhs + r, acc);
+    batch_hop_pair<FMT, RECON, ISIGN, NRHS, 0>(P, h, r, n, acc);
+    batch_hop_pair<FMT, RECON, ISIGN, NRHS, 1>(P, h, r, n, acc);
+    batch_hop_pair<FMT, RECON, ISIGN, NRHS, 2>(P, h, r, n, acc);
+    batch_hop_pair<FMT, RECON, ISIGN, NRHS, 3>(P, h, r, n, acc);
+    Sio<FMT>::store(P.res, P.cs, (size_t)h * nr + r, acc);
 }
 
+
 template <int FMT, int RECON>
-__global__ void __launch_bounds__(256, 3) batch_kernel(const Problem *__restrict__ probs, const Tile *__restrict__ tiles,
+__global__ void __launch_bounds__(256, 3) batch_kernel(const __grid_constant__ BatchParams bp, const Tile *__restrict__ tiles,
                                                     int ntiles) {
     for (int w = blockIdx.x; w < ntiles; w += gridDim.x) {
         const Tile tl = tiles[w];
-        const Problem &P = probs[tl.problem];
+        const Problem &P = bp.p[tl.problem];
         const int t = tl.first + threadIdx.x;
         if (t < tl.end) {
-            if (P.isign > 0) batch_site<FMT, RECON, 1>(P, t);
-            else batch_site<FMT, RECON, -1>(P, t);
+            // the count of right-hand sides stays a run-time value: one body
+            // per isign keeps the register budget of the single-lattice kernel
+            if (P.isign > 0) batch_site<FMT, RECON, 1, 0>(P, t);
+            else batch_site<FMT, RECON, -1, 0>(P, t);
         }
     }
 }
@@ -95,7 +108,7 @@ struct gbds_batch_s {
     int block = 128;     // threads per tile
     int grid = 0;        // resident CTAs (0: one per tile up to the machine size)
     int order = 0;       // 0: tiles of one lattice after another; 1: interleaved across lattices
-    Problem *d_probs = nullptr;
+    BatchParams params;
     Tile *d_tiles = nullptr;
     int ntiles = 0;
     int sms = 0;
@@ -145,7 +158,7 @@ int build_tiles(gbds_batch b) {
 cudaError_t launch_batch(gbds_batch b, cudaStream_t st) {
     int grid = b->grid > 0 ? b->grid : b->ntiles;
     grid = std::max(1, std::min(grid, b->ntiles));
-#define GBDS_B(F, R) batch_kernel<F, R><<<grid, b->block, 0, st>>>(b->d_probs, b->d_tiles, b->ntiles)
+#define GBDS_B(F, R) batch_kernel<F, R><<<grid, b->block, 0, st>>>(b->params, b->d_tiles, b->ntiles)
     if (b->recon == 18) {
         if (b->format == 0) GBDS_B(kFmtNative, 18); else if (b->format == 1) GBDS_B(kFmtBF16, 18); else GBDS_B(kFmtF16N, 18);
     } else {
@@ -160,6 +173,7 @@ cudaError_t launch_batch(gbds_batch b, cudaStream_t st) {
 
 extern "C" int gbds_batch_create(gbds_batch *out, const gbds_batch_item *items, int n, int recon, int format) {
     if (!out || !items || n <= 0) return set_error(GBDS_ERROR_INVALID_VALUE, "need at least one batch item");
+    if (n > kMaxBatch) return set_error(GBDS_ERROR_INVALID_VALUE, "at most 32 lattices per batch");
     *out = nullptr;
     if (recon != 18 && recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "recon must be 18 or 12");
     if (format < 0 || format > 2) return set_error(GBDS_ERROR_INVALID_VALUE, "unknown spinor format");
@@ -193,17 +207,10 @@ extern "C" int gbds_batch_create(gbds_batch *out, const gbds_batch_item *items, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
     b->grid = b->sms * 4;
-    cudaError_t e = cudaMalloc(&b->d_probs, sizeof(Problem) * b->probs.size());
-    if (e == cudaSuccess)
-        e = cudaMemcpy(b->d_probs, b->probs.data(), sizeof(Problem) * b->probs.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        if (b->d_probs) cudaFree(b->d_probs);
-        delete b;
-        return cuda_error(e, "gbds_batch_create");
-    }
+    b->params.n = n;
+    for (int i = 0; i < n; i++) b->params.p[i] = b->probs[i];
     int rc = build_tiles(b);
     if (rc != GBDS_SUCCESS) {
-        cudaFree(b->d_probs);
         delete b;
         return rc;
     }
@@ -214,7 +221,6 @@ extern "C" int gbds_batch_create(gbds_batch *out, const gbds_batch_item *items, 
 extern "C" int gbds_batch_destroy(gbds_batch b) {
     if (!b) return GBDS_SUCCESS;
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    if (b->d_probs) cudaFree(b->d_probs);
     if (b->d_tiles) cudaFree(b->d_tiles);
     delete b;
     return GBDS_SUCCESS;

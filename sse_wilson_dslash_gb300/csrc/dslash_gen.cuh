@@ -94,6 +94,21 @@ struct Sio<kFmtF16N> {
     __device__ __forceinline__ static const float *norms(const char *base, size_t cs) {
         return reinterpret_cast<const float *>(base + 3 * 16 * cs);
     }
+    // the stored halves, not multiplied by the norm (values in [-1, 1])
+    __device__ __forceinline__ static void load_raw(const char *base, size_t cs, size_t i, cx<float> (&s)[4][3]) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint4 q = __ldg(p + k * cs + i);
+            const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[c]));
+                const int j = 4 * k + c;
+                s[j / 3][j % 3] = {f.x, f.y};
+            }
+        }
+    }
     __device__ __forceinline__ static void load(const char *base, size_t cs, size_t i, cx<float> (&s)[4][3]) {
         const uint4 *p = reinterpret_cast<const uint4 *>(base);
         const float nrm = __ldg(norms(base, cs) + i);

@@ -428,26 +428,22 @@ cudaError_t launch_dslash_xpay_t(const Geom &g, int recon, const void *gauge, co
     return cudaGetLastError();
 }
 
+// A template (not explicit specialisations), so that the variant kernels are
+// instantiated only in the translation units that launch them.
 template <typename T>
-void launch_minb(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, int minb, cudaStream_t s);
-
-template <>
-inline void launch_minb<float>(const DslashArgs<float> &a, dim3 grid, int block, int nd, int recon, int isign, int minb,
-                               cudaStream_t s) {
-    switch (minb) {
-    case 6: launch_variant<float, 6>(a, grid, block, nd, recon, isign, s); break;
-    case 7: launch_variant<float, 7>(a, grid, block, nd, recon, isign, s); break;
-    case 8: launch_variant<float, 8>(a, grid, block, nd, recon, isign, s); break;
-    default: launch_variant<float, 10>(a, grid, block, nd, recon, isign, s); break;
-    }
-}
-
-template <>
-inline void launch_minb<double>(const DslashArgs<double> &a, dim3 grid, int block, int nd, int recon, int isign,
-                                int minb, cudaStream_t s) {
-    switch (minb) {
-    case 3: launch_variant<double, 3>(a, grid, block, nd, recon, isign, s); break;
-    default: launch_variant<double, 4>(a, grid, block, nd, recon, isign, s); break;
+void launch_minb(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, int minb, cudaStream_t s) {
+    if constexpr (sizeof(T) == 4) {
+        switch (minb) {
+        case 6: launch_variant<T, 6>(a, grid, block, nd, recon, isign, s); break;
+        case 7: launch_variant<T, 7>(a, grid, block, nd, recon, isign, s); break;
+        case 8: launch_variant<T, 8>(a, grid, block, nd, recon, isign, s); break;
+        default: launch_variant<T, 10>(a, grid, block, nd, recon, isign, s); break;
+        }
+    } else {
+        switch (minb) {
+        case 3: launch_variant<T, 3>(a, grid, block, nd, recon, isign, s); break;
+        default: launch_variant<T, 4>(a, grid, block, nd, recon, isign, s); break;
+        }
     }
 }
 

@@ -70,6 +70,10 @@ cudaError_t launch_pack_gen_half(int fmt, const Geom &g, int nrhs, const float *
 cudaError_t launch_unpack_gen_half(int fmt, const Geom &g, int nrhs, const void *in, const int *table, int parity,
                                    float *packed, cudaStream_t st);
 inline int gen_spinor_bytes(int fmt) { return fmt == 0 ? 96 : (fmt == 1 ? 48 : 52); }
+// Tensor-core form (dslash_tc.cu): fmt 1 / 2, nrhs 16 or 32, FP32 links
+// converted to the 16-bit operand type; err set to 1 on a timed-out wait.
+cudaError_t launch_gen_tc(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,
+                          int isign, int cb, int *err, cudaStream_t st);
 // nrhs 1, 16-bit spinors (fmt 1 / 2) with FP16 links: gauge is the FP32
 // internal gauge converted by convert_links_f16 (recon * 2 bytes per link
 // per site-stride).
@@ -94,5 +98,7 @@ struct gbds_op_s {
     int variant;
     int nrhs;    // right-hand sides per site (1 = the plain operator)
     int format;  // spinor storage: 0 native (prec), 1 bfloat16, 2 half + per-spinor norm
+    int tensor_cores;  // 16-bit formats, nrhs 16/32: colour multiply on tcgen05
+    int *d_err;        // device flag of the tensor-core kernel's bounded waits
     int *d_site_table;  // device copy of the layout table, or nullptr (canonical)
 };

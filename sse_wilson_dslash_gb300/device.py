@@ -82,6 +82,14 @@ class DslashOperator:
     def canonical(self) -> bool:
         return bool(_lib.core().gbds_op_is_canonical(self._h))
 
+    def set_tensor_cores(self, on: bool = True) -> None:
+        """Colour multiply on the tensor cores (16-bit formats, nrhs 16 or 32)."""
+        _lib.check(_lib.core().gbds_op_set_tensor_cores(self._h, 1 if on else 0))
+
+    def check(self) -> None:
+        """Synchronise; raise if a tensor-core launch timed out."""
+        _lib.check(_lib.core().gbds_op_check(self._h))
+
     def set_tuning(self, threads: int, variant: int = 0) -> None:
         _lib.check(_lib.core().gbds_op_set_tuning(self._h, int(threads), int(variant)))
 

@@ -63,3 +63,48 @@ def test_multi_rhs_bytes_accounting():
     assert op.bytes_per_site == 2 * 48 + 8 * 48 / 16
     assert op.spinor_bytes == 48 * op.stride * 16
     op.close()
+
+
+# Tensor-core form: besides the storage rounding above, the projected half
+# spinor and the link enter the MMA rounded to the 16-bit operand type (one
+# more rounding of each, FP32 accumulation), well inside the same per-site
+# bounds.
+@pytest.mark.parametrize("fmt", ["bf16", "f16"])
+@pytest.mark.parametrize("nrhs", [16, 32])
+def test_tensor_core_multi_rhs_matches_oracle(nrhs, fmt):
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims = (8, 4, 6, 4)
+    V = O.volume(dims)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    rng = np.random.default_rng(100 + nrhs)
+    u = O.random_gauge(rng, V)
+    psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
+    for recon in (18, 12):
+        op = DslashOperator(dims, nd=4, prec=32, recon=recon, nrhs=nrhs, spinor_format=fmt)
+        op.set_tensor_cores(True)
+        gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
+        packed = torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda()
+        for isign, cb in ((1, 0), (-1, 1), (1, 1), (-1, 0)):
+            src = op.pack_spinor(packed, cb)
+            out = op.apply(gauge, src, isign, cb)
+            op.check()
+            res = torch.zeros(nrhs * V * 24, dtype=torch.float32, device="cuda")
+            op.unpack_spinor(out, 1 - cb, res)
+            got = res.cpu().numpy().reshape(nrhs, V, 24)
+            ts = O.target_sites(4, dims, lol, cb)
+            for r in range(nrhs):
+                ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
+                err = O.site_rel_err(got[r], ref, ts)
+                assert err <= TOL[fmt], (recon, isign, cb, r, err)
+        op.close()
+
+
+def test_tensor_cores_need_16bit_and_16_or_32_rhs():
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    from sse_wilson_dslash_gb300 import _lib
+    for nrhs, fmt in ((32, "native"), (8, "bf16"), (1, "f16")):
+        op = DslashOperator((4, 4, 4, 4), nrhs=nrhs, spinor_format=fmt)
+        with pytest.raises(_lib.GbdsError):
+            op.set_tensor_cores(True)
+        op.close()
