@@ -151,8 +151,11 @@ int gbds_op_num_variants(gbds_op op);
 
 /* Time every (block, variant) candidate of gbds_op_dslash on the caller's
  * fields (res is overwritten), keep the fastest for this operator and cache
- * it process-wide for its (dims, nd, prec, recon); a later call for the same
- * shape takes the cached choice without timing.  Synchronises `stream`. */
+ * it process-wide for its (dims, nd, prec, recon, nrhs, format); a later call
+ * for the same shape takes the cached choice without timing.  For 16-bit
+ * formats with 16 or 32 right-hand sides the candidates are the CUDA-core and
+ * the tensor-core kernels (gbds_op_set_tensor_cores); other operators with
+ * several right-hand sides have nothing to tune.  Synchronises `stream`. */
 int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream);
 
 /* Number of kernels this library has launched in this process (all kinds). */

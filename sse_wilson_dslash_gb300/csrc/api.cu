@@ -225,41 +225,61 @@ extern "C" int gbds_op_num_variants(gbds_op op) { return op ? dslash_variants(op
 
 namespace {
 std::mutex g_tune_mutex;
-std::map<std::array<int, 7>, std::array<int, 2>> g_tune_cache;  // (dims, nd, prec, recon) -> (block, variant)
+// (dims, nd, prec, recon, nrhs, format) -> (block, variant, tensor cores)
+std::map<std::array<int, 9>, std::array<int, 3>> g_tune_cache;
+}  // namespace
+
+static bool tc_eligible(gbds_op op) {
+    return op->format != GBDS_SPINOR_NATIVE && (op->nrhs == 16 || op->nrhs == 32);
 }
 
 extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream) {
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
-    const std::array<int, 7> key = {op->g.L[0], op->g.L[1], op->g.L[2], op->g.L[3], op->g.nd, op->prec, op->recon};
+    // several right-hand sides: the kernels take no block / variant choice;
+    // 16-bit storage with 16 or 32 of them chooses CUDA cores or tensor cores
+    if (generic(op) && !tc_eligible(op)) return GBDS_SUCCESS;
+    const std::array<int, 9> key = {op->g.L[0], op->g.L[1], op->g.L[2], op->g.L[3], op->g.nd,
+                                    op->prec,   op->recon,  op->nrhs,   op->format};
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
             op->block = it->second[0];
             op->variant = it->second[1];
-            return GBDS_SUCCESS;
+            return it->second[2] ? gbds_op_set_tensor_cores(op, 1) : gbds_op_set_tensor_cores(op, 0);
         }
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    std::vector<std::array<int, 2>> cand = {{64, 0}, {128, 0}, {256, 0}};
-    for (int v = 1; v < dslash_variants(op->prec); v++) cand.push_back({128, v});
+    std::vector<std::array<int, 3>> cand;
+    if (generic(op)) {
+        cand = {{op->block, op->variant, 0}, {op->block, op->variant, 1}};
+    } else {
+        cand = {{64, 0, 0}, {128, 0, 0}, {256, 0, 0}};
+        for (int v = 1; v < dslash_variants(op->prec); v++) cand.push_back({128, v, 0});
+    }
     cudaEvent_t e0, e1;
     cudaError_t e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e != cudaSuccess) return cuda_error(e, "autotune events");
     float best = 1e30f;
-    std::array<int, 2> pick = {op->block, op->variant};
+    std::array<int, 3> pick = {op->block, op->variant, op->tensor_cores};
     const int reps = op->prec == 32 ? 10 : 3;
+    int rc = GBDS_SUCCESS;
     for (const auto &c : cand) {
         op->block = c[0];
         op->variant = c[1];
-        int rc = gbds_op_dslash(op, gauge, psi, res, 1, 0, stream);  // warm-up
-        if (rc != GBDS_SUCCESS) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+        rc = gbds_op_set_tensor_cores(op, c[2]);
+        if (rc == GBDS_SUCCESS) rc = gbds_op_dslash(op, gauge, psi, res, 1, 0, stream);  // warm-up
+        if (rc != GBDS_SUCCESS) break;
         cudaEventRecord(e0, s);
         for (int r = 0; r < reps; r++) gbds_op_dslash(op, gauge, psi, res, (r & 1) ? -1 : 1, 0, stream);
         cudaEventRecord(e1, s);
         e = cudaEventSynchronize(e1);
         if (e != cudaSuccess) break;
+        if (c[2]) {
+            rc = gbds_op_check(op);  // a timed-out tensor-core wait disqualifies the candidate
+            if (rc != GBDS_SUCCESS) break;
+        }
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         if (ms < best) { best = ms; pick = c; }
@@ -267,8 +287,11 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_error(e, "autotune");
+    if (rc != GBDS_SUCCESS) return rc;
     op->block = pick[0];
     op->variant = pick[1];
+    rc = gbds_op_set_tensor_cores(op, pick[2]);
+    if (rc != GBDS_SUCCESS) return rc;
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     g_tune_cache[key] = pick;
     return GBDS_SUCCESS;

@@ -1,29 +1,37 @@
 // Several right-hand sides with the SU(3) multiply on the tensor cores
-// (tcgen05.mma, accumulators in TMEM), 16-bit spinor storage.
+// (tcgen05.mma, A in TMEM, accumulators in TMEM), 16-bit spinor storage.
 //
-// For one hop of one site, the colour multiply of all NRHS right-hand sides
-// is a real matrix product: with H the projected half spinors as rows
-// (rhs r, spin half s) of 6 reals (3 colours x re/im) and U the link in its
-// real 6x6 form,  W^T = H^T U^T  (rows (r, s), 6 output reals).  One
-// tcgen05.mma (M = 128, K = 16, kind::f16: bf16 or f16 operands, FP32
-// accumulation) takes P = 128 / (2 NRHS) sites at once: A holds the P blocks
-// of 2 NRHS rows; B holds the P links side by side (N = 8 P: 6 used columns
-// per site), so block (p, p) of D is site p's result and the other blocks are
-// not read.  K = 16 carries the 6 used reals plus zeros.
+// For one direction mu of one site, the colour multiplies of all NRHS
+// right-hand sides are one real matrix product.  Row (site p, rhs r) of A
+// holds, in K = 32 (bf16 or f16, four k-groups of 8), the projected half
+// spinors of the neighbours: k-group 0 = forward half 0, 1 = forward half 1,
+// 2 = backward half 0, 3 = backward half 1 (6 reals each, 2 zeros).  B holds,
+// per site, 24 rows (the output columns of D):
+//   rows 0..5   SUM  half 0:  [M_f | 0 | M_b | 0]
+//   rows 6..11  SUM  half 1:  [0 | M_f | 0 | M_b]
+//   rows 12..17 DIFF half 0:  [M_f | 0 | -M_b | 0]
+//   rows 18..23 DIFF half 1:  [0 | M_f | 0 | -M_b]
+// with M_f the real 6x6 form of U_mu(x) and M_b that of U_mu(x - mu)^dagger.
+// The forward and backward projectors differ only in the sign of gamma_mu,
+// so the upper spin components take the sums and the lower components
+// (+-1 or +-i) times the differences.  One pair of MMAs (M = 128, N = 24 P,
+// K = 2 x 16) serves both hops of a direction for P = 128 / NRHS sites; each
+// row reads back only its own site's 24 columns of D.
 //
-// A CTA of 128 threads owns P consecutive sites; thread t is A row t:
-// (site p, rhs r, spin half s).  Per round of HR hops it loads and projects
-// the neighbour spinors (CUDA cores), writes its A rows, writes the links
-// into B, and one thread issues HR MMAs into HR column blocks of TMEM and
-// commits them to an mbarrier; after the (bounded) wait every thread reads
-// its D row back with tcgen05.ld and reconstructs the four spin components
-// (CUDA cores).  Spin halves s = 0, 1 of one rhs sit in adjacent lanes and
-// combine their partial lower spin components with a shuffle at the end.
+// Kernel structure: persistent CTAs of 128 threads (thread t = row t) walk
+// tiles of P sites, four rounds (mu = 0..3) per tile.  A round: projection
+// of the neighbour spinors (loaded into registers during the round before)
+// in packed 16-bit arithmetic, the A row to TMEM (tcgen05.st), the B rows of
+// each site to shared memory (six link-row threads per site), the loads of
+// the next round, one thread issuing the MMAs and waiting (bounded) on their
+// mbarrier while the others wait at a CTA barrier, and the D rows read back
+// (tcgen05.ld) and folded into the output spinor in registers (FP32).
 //
-// Operand layout in shared memory: K-major, no swizzle, core matrices of
-// 8 rows x 16 bytes; element (row, k) at ((row/8)*2 + k/8)*128 + (row%8)*16 +
-// (k%8)*2; descriptors with leading (K) byte offset 128 and stride (8-row)
-// byte offset 256.
+// Shared-memory operand layout (B): K-major, no swizzle, core matrices of
+// 8 rows x 16 bytes; element (row, k) at (row/8)*512 + (k/8)*128 +
+// (row%8)*16 + (k%8)*2; descriptor leading (K) byte offset 128, stride
+// (8-row) byte offset 512.  TMEM operand layout (A): lane = row, two 16-bit
+// elements per 32-bit column, k ascending, even k in the low half.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -41,136 +49,431 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     uint64_t d = 0;
     d |= (uint64_t)((addr >> 4) & 0x3FFF);
     d |= (uint64_t)(128 >> 4) << 16;  // K-direction core-matrix offset
-    d |= (uint64_t)(256 >> 4) << 32;  // 8-row core-matrix offset
+    d |= (uint64_t)(512 >> 4) << 32;  // 8-row core-matrix offset
     d |= (uint64_t)1 << 46;           // descriptor version for tcgen05
     return d;
 }
 
-// Offset of the first 16 bytes (k = 0..7) of row r in a K-major operand.
-__device__ __forceinline__ int row_off(int r) { return (r / 8) * 256 + (r % 8) * 16; }
+// Byte offset of the 16-byte core row (row, k-group kg) of the K = 32 B operand.
+__device__ __forceinline__ int core_off(int row, int kg) { return (row >> 3) * 512 + kg * 128 + (row & 7) * 16; }
 
-template <int FMT>
-__device__ __forceinline__ uint32_t pack2(float a, float b) {
-    if constexpr (FMT == kFmtBF16) {
+// Packed two-element 16-bit arithmetic (one complex number per 32 bits).
+template <int FMT> struct Pk;
+template <> struct Pk<kFmtBF16> {
+    static constexpr uint32_t kOne = 0x3F80u;
+    __device__ __forceinline__ static uint32_t fma2(uint32_t a, uint32_t b, uint32_t c) {
+        const __nv_bfloat162 r = __hfma2(*reinterpret_cast<const __nv_bfloat162 *>(&a),
+                                         *reinterpret_cast<const __nv_bfloat162 *>(&b),
+                                         *reinterpret_cast<const __nv_bfloat162 *>(&c));
+        return *reinterpret_cast<const uint32_t *>(&r);
+    }
+    __device__ __forceinline__ static uint32_t mul2(uint32_t a, uint32_t b) {
+        const __nv_bfloat162 r = __hmul2(*reinterpret_cast<const __nv_bfloat162 *>(&a),
+                                         *reinterpret_cast<const __nv_bfloat162 *>(&b));
+        return *reinterpret_cast<const uint32_t *>(&r);
+    }
+    __device__ __forceinline__ static uint32_t pack(float a, float b) {
         const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
         return *reinterpret_cast<const uint32_t *>(&v);
-    } else {
+    }
+};
+template <> struct Pk<kFmtF16N> {
+    static constexpr uint32_t kOne = 0x3C00u;
+    __device__ __forceinline__ static uint32_t fma2(uint32_t a, uint32_t b, uint32_t c) {
+        const __half2 r = __hfma2(*reinterpret_cast<const __half2 *>(&a), *reinterpret_cast<const __half2 *>(&b),
+                                  *reinterpret_cast<const __half2 *>(&c));
+        return *reinterpret_cast<const uint32_t *>(&r);
+    }
+    __device__ __forceinline__ static uint32_t mul2(uint32_t a, uint32_t b) {
+        const __half2 r = __hmul2(*reinterpret_cast<const __half2 *>(&a), *reinterpret_cast<const __half2 *>(&b));
+        return *reinterpret_cast<const uint32_t *>(&r);
+    }
+    __device__ __forceinline__ static uint32_t pack(float a, float b) {
         const __half2 v = __floats2half2_rn(a, b);
         return *reinterpret_cast<const uint32_t *>(&v);
     }
+};
+
+// Multiplier vector (re, im) for coefficient code 0: +1, 1: -1, 2: +i, 3: -i,
+// applied to a half-swapped operand for codes 2 and 3.
+template <int FMT, int CODE>
+__device__ __forceinline__ constexpr uint32_t coef_vec() {
+    constexpr uint32_t one = Pk<FMT>::kOne, neg = Pk<FMT>::kOne | 0x8000u;
+    return CODE == 0 ? (one | (one << 16))
+         : CODE == 1 ? (neg | (neg << 16))
+         : CODE == 2 ? (neg | (one << 16))   // (re, im) -> (-im, re)
+                     : (one | (neg << 16));  // (re, im) -> (im, -re)
 }
 
-template <int NRHS, int HR>
+template <int CODE>
+__device__ __forceinline__ uint32_t coef_operand(uint32_t w) {
+    return CODE >= 2 ? __byte_perm(w, 0, 0x1032) : w;  // swap re and im
+}
+
+// Both half spinors of one full spinor (w[3a + c] = spin a, colour c) for
+// the projector (1 - SIGMA gamma_mu).
+template <int FMT, int MU, int SIGMA>
+__device__ __forceinline__ void project_packed(const uint4 (&q)[3], uint32_t (&h0)[3], uint32_t (&h1)[3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIGMA > 0 ? 0 : 1;
+    const uint32_t w[12] = {q[0].x, q[0].y, q[0].z, q[0].w, q[1].x, q[1].y, q[1].z, q[1].w, q[2].x, q[2].y, q[2].z, q[2].w};
+    constexpr uint32_t v0 = coef_vec<FMT, P::a0 ^ f>(), v1 = coef_vec<FMT, P::a1 ^ f>();
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        h0[c] = Pk<FMT>::fma2(coef_operand<P::a0>(w[3 * P::j0 + c]), v0, w[c]);
+        h1[c] = Pk<FMT>::fma2(coef_operand<P::a1>(w[3 * P::j1 + c]), v1, w[3 + c]);
+    }
+}
+
+// n / d for 0 <= n < 2^31 by multiply-high: q = umulhi(n, m) >> s.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+
+FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f{d, 0u, 0u};
+    if (d <= 1) return f;
+    uint32_t l = 0;
+    while ((1ull << l) < d) l++;  // l = ceil(log2 d) >= 1
+    // m = ceil(2^(31 + l) / d) < 2^32; error < 2^-l <= 1/d for n < 2^31
+    f.m = (uint32_t)(((1ull << (31 + l)) + d - 1) / d);
+    f.s = l - 1;
+    return f;
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) { return f.d <= 1 ? n : __umulhi(n, f.m) >> f.s; }
+
+template <int NRHS>
 struct TcShape {
-    static constexpr int P = 128 / (2 * NRHS);  // sites per CTA
-    static constexpr int N = 8 * P;             // MMA N
-    static constexpr int COLS = HR * N;         // TMEM columns
-    static constexpr int A_BYTES = 128 * 32;
-    static constexpr int B_BYTES = N * 32;
-    static constexpr int SMEM = HR * (A_BYTES + B_BYTES);
+    static constexpr int P = 128 / NRHS;                   // sites per tile
+    static constexpr int N = 24 * P;                       // MMA N (D columns)
+    static constexpr int ACOL = N;                         // first A column in TMEM
+    static constexpr int COLS = N + 16 <= 128 ? 128 : 256;  // TMEM allocation
+    static constexpr int B_BYTES = N * 64;
 };
 
 struct TcArgs {
     Geom g;
+    FastDiv dx, dy, dz;  // Lx/2, Ly, Lz
     const char *psi, *gauge;
     char *res;
     size_t link_block_bytes;
-    size_t cs;
-    int pt;
+    size_t cs;  // uint4 elements between the three spinor component arrays
+    int pt;     // target checkerboard
+    int ntiles;
     int *err;
 };
 
-// Hop index 0..7 -> (mu, forward?)
-template <int FMT, int RECON, int ISIGN, int NRHS, int HOP>
-__device__ __forceinline__ void tc_prepare(const TcArgs &a, bool active, int h, int r, int s, int p, int j,
-                                           const Nbr &n, unsigned char *A, unsigned char *B) {
-    constexpr int MU = HOP / 2;
-    constexpr bool FWD = (HOP % 2) == 0;
-    constexpr int SIGMA = FWD ? ISIGN : -ISIGN;
-    using Pj = Proj<MU>;
-    constexpr int f = SIGMA > 0 ? 0 : 1;
-    const int t = threadIdx.x;
-    // --- A row: projected half spinor component s of the neighbour, rhs r
-    uint4 row = make_uint4(0, 0, 0, 0);
-    if (active) {
-        const int nb = FWD ? n.f[MU] : n.b[MU];
-        cx<float> sp[4][3];
-        // half + norm: the normalised halves go to the tensor core and the
-        // norm scales the result rows afterwards
-        if constexpr (FMT == kFmtF16N) Sio<FMT>::load_raw(a.psi, a.cs, (size_t)nb * NRHS + r, sp);
-        else Sio<FMT>::load(a.psi, a.cs, (size_t)nb * NRHS + r, sp);
-        cx<float> hv[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const cx<float> h0 = cadd(sp[0][c], mulc<Pj::a0 ^ f>(sp[Pj::j0][c]));
-            const cx<float> h1 = cadd(sp[1][c], mulc<Pj::a1 ^ f>(sp[Pj::j1][c]));
-            hv[c] = s == 0 ? h0 : h1;
-        }
-        row = make_uint4(pack2<FMT>(hv[0].r, hv[0].i), pack2<FMT>(hv[1].r, hv[1].i), pack2<FMT>(hv[2].r, hv[2].i), 0u);
+// A target site and its coordinates.
+struct Co {
+    int h, x, y, z, t;
+};
+
+__device__ __forceinline__ Co coords(const TcArgs &a, int h) {
+    Co c;
+    c.h = h;
+    const uint32_t r1 = fdiv((uint32_t)h, a.dx);
+    const int xh = h - (int)r1 * a.g.Lxh;
+    const uint32_t r2 = fdiv(r1, a.dy);
+    c.y = (int)r1 - (int)r2 * a.g.L[1];
+    c.t = (int)fdiv(r2, a.dz);
+    c.z = (int)r2 - c.t * a.g.L[2];
+    c.x = 2 * xh + ((c.y + c.z + c.t + a.pt) & 1);
+    return c;
+}
+
+// Forward and backward neighbours of c in direction MU (periodic).
+template <int MU>
+__device__ __forceinline__ void nbr(const Geom &g, const Co &c, int &f, int &b) {
+    if constexpr (MU == 0) {
+        const int row = c.h - (c.x >> 1);
+        const int xp = (c.x + 1 == g.L[0]) ? 0 : c.x + 1;
+        const int xm = (c.x == 0) ? g.L[0] - 1 : c.x - 1;
+        f = row + (xp >> 1);
+        b = row + (xm >> 1);
+    } else {
+        const int L = g.L[MU];
+        const int crd = MU == 1 ? c.y : (MU == 2 ? c.z : c.t);
+        const int st = MU == 1 ? g.Lxh : (MU == 2 ? g.Lxh * g.L[1] : g.Lxh * g.L[1] * g.L[2]);
+        f = (crd + 1 == L) ? c.h - (L - 1) * st : c.h + st;
+        b = (crd == 0) ? c.h + (L - 1) * st : c.h - st;
     }
-    *reinterpret_cast<uint4 *>(A + row_off(t)) = row;
-    // --- B row j of site p: output real j = 2*c + (0 re, 1 im) over input reals k = 2*ci + (0 re, 1 im)
-    if (j < 8) {
-        uint4 brow = make_uint4(0, 0, 0, 0);
-        if (active && j < 6) {
-            cx<float> U[3][3];
-            const int lh = FWD ? h : n.b[MU];
-            const int lp = FWD ? a.pt : 1 - a.pt;
-            Field<float>::template load_link<RECON>(a.gauge + (size_t)(lp * 4 + MU) * a.link_block_bytes, a.g.stride, lh, U);
-            const int c = j / 2;
-            const bool im = j & 1;
-            float v[6];
+}
+
+// One round's inputs of a thread, loaded a round ahead.
+struct Raw {
+    uint4 qf[3], qb[3];  // forward and backward neighbour spinors (rhs r)
+    float nf, nb;        // their norms (half + norm format)
+    float l[12];         // link data (link-row threads): recon 18 -> 3 complex, recon 12 -> rows 0 and 1
+};
+
+// Link-row thread: complex entries M[c][ci] (ci = 0..2) of M = U_mu(x)
+// (dir 0) or U_mu(x - mu)^dagger (dir 1) from the loaded link data.
+template <int RECON>
+__device__ __forceinline__ void link_row(const float (&l)[12], int dir, int c, float (&mr)[3], float (&mi)[3]) {
+    if constexpr (RECON == 18) {
+        // loaded: U[c][ci] (dir 0) or U[ci][c] (dir 1)
+        const float sg = dir == 0 ? 1.f : -1.f;
 #pragma unroll
-            for (int ci = 0; ci < 3; ci++) {
-                // M = U (forward) or U^dagger (backward); M[c][ci]
-                const float mr = FWD ? U[c][ci].r : U[ci][c].r;
-                const float mi = FWD ? U[c][ci].i : -U[ci][c].i;
-                // re out: mr*hr - mi*hi ; im out: mi*hr + mr*hi
-                v[2 * ci] = im ? mi : mr;
-                v[2 * ci + 1] = im ? mr : -mi;
+        for (int ci = 0; ci < 3; ci++) {
+            mr[ci] = l[2 * ci];
+            mi[ci] = sg * l[2 * ci + 1];
+        }
+    } else {
+        cx<float> U[3][3];
+#pragma unroll
+        for (int k = 0; k < 6; k++) U[k / 3][k % 3] = {l[2 * k], l[2 * k + 1]};
+        reconstruct_row2(U);
+#pragma unroll
+        for (int ci = 0; ci < 3; ci++) {
+            // dir 0: U[c][ci]; dir 1: conj(U[ci][c])
+            const cx<float> f = c == 0 ? U[0][ci] : (c == 1 ? U[1][ci] : U[2][ci]);
+            const cx<float> b = c == 0 ? U[ci][0] : (c == 1 ? U[ci][1] : U[ci][2]);
+            mr[ci] = dir == 0 ? f.r : b.r;
+            mi[ci] = dir == 0 ? f.i : -b.i;
+        }
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t *d);
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, uint32_t *d) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7])
+                 : "r"(taddr));
+}
+template <>
+__device__ __forceinline__ void tmem_ld<16>(uint32_t taddr, uint32_t *d) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+                   "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15])
+                 : "r"(taddr));
+}
+
+template <int FMT, int RECON, int ISIGN, int NRHS>
+struct TcCta {
+    using S = TcShape<NRHS>;
+    const TcArgs &a;
+    int t, w, p, r, dir, c;
+    bool item;  // link-row thread: B rows (dir, colour c) of its site
+    unsigned char *B;
+    const uint4 *ps;  // spinor base of rhs r
+
+    __device__ __forceinline__ TcCta(const TcArgs &args, unsigned char *sb) : a(args), B(sb) {
+        t = threadIdx.x;
+        w = t >> 5;
+        p = t / NRHS;
+        r = t % NRHS;
+        item = r < 6;
+        dir = r / 3;
+        c = r % 3;
+        ps = reinterpret_cast<const uint4 *>(a.psi) + r;
+    }
+
+    template <int MU>
+    __device__ __forceinline__ void load(const Co &co, bool act, Raw &raw) const {
+        if (!act) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) raw.qf[k] = raw.qb[k] = make_uint4(0, 0, 0, 0);
+            raw.nf = raw.nb = 0.f;
+#pragma unroll
+            for (int k = 0; k < 12; k++) raw.l[k] = 0.f;
+            return;
+        }
+        int f, b;
+        nbr<MU>(a.g, co, f, b);
+        const uint4 *pf = ps + (size_t)f * NRHS;
+        const uint4 *pb = ps + (size_t)b * NRHS;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            raw.qf[k] = __ldg(pf + k * a.cs);
+            raw.qb[k] = __ldg(pb + k * a.cs);
+        }
+        if constexpr (FMT == kFmtF16N) {
+            const float *nr = Sio<kFmtF16N>::norms(a.psi, a.cs) + r;
+            raw.nf = __ldg(nr + (size_t)f * NRHS);
+            raw.nb = __ldg(nr + (size_t)b * NRHS);
+        }
+        if (item) {
+            const char *blk = a.gauge + (size_t)((dir == 0 ? a.pt : 1 - a.pt) * 4 + MU) * a.link_block_bytes;
+            const size_t ls = (size_t)(dir == 0 ? co.h : b);
+            const size_t stride = (size_t)a.g.stride;
+            if constexpr (RECON == 18) {
+                const float2 *pl = reinterpret_cast<const float2 *>(blk) + ls;
+                const size_t step = (dir == 0 ? 1 : 3) * stride;
+                const float2 *p0 = pl + (size_t)(dir == 0 ? 3 * c : c) * stride;
+#pragma unroll
+                for (int ci = 0; ci < 3; ci++) {
+                    const float2 v = __ldg(p0 + ci * step);
+                    raw.l[2 * ci] = v.x;
+                    raw.l[2 * ci + 1] = v.y;
+                }
+            } else {
+                const float4 *pl = reinterpret_cast<const float4 *>(blk) + ls;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const float4 v = __ldg(pl + k * stride);
+                    raw.l[4 * k] = v.x;
+                    raw.l[4 * k + 1] = v.y;
+                    raw.l[4 * k + 2] = v.z;
+                    raw.l[4 * k + 3] = v.w;
+                }
             }
-            brow = make_uint4(pack2<FMT>(v[0], v[1]), pack2<FMT>(v[2], v[3]), pack2<FMT>(v[4], v[5]), 0u);
         }
-        *reinterpret_cast<uint4 *>(B + row_off(p * 8 + j)) = brow;
     }
-}
 
-template <int ISIGN, int HOP>
-__device__ __forceinline__ void tc_reconstruct(int s, const cx<float> (&w)[3], cx<float> (&up)[3], cx<float> (&l2)[3],
-                                               cx<float> (&l3)[3]) {
-    constexpr int MU = HOP / 2;
-    constexpr bool FWD = (HOP % 2) == 0;
-    constexpr int SIGMA = FWD ? ISIGN : -ISIGN;
-    using Pj = Proj<MU>;
-    constexpr int f = SIGMA > 0 ? 0 : 1;
-    // this half spinor (index s) feeds upper component s and the lower
-    // component whose source index (k2 or k3) equals s
-    const bool to2 = (Pj::k2 == s);
+    // L1 prefetch of round MU's spinors and links (two rounds ahead of use,
+    // one round ahead of the register loads, which then hit L1), for 16
+    // right-hand sides.
+    template <int MU>
+    __device__ __forceinline__ void prefetch(const Co &co, bool act) const {
+        // measured: pays off with two sites per warp (16 right-hand sides),
+        // costs more issue slots than it saves with one (32)
+        if constexpr (NRHS >= 32) return;
+        if (!act) return;
+        int f, b;
+        nbr<MU>(a.g, co, f, b);
+        const uint4 *pf = ps + (size_t)f * NRHS;
+        const uint4 *pb = ps + (size_t)b * NRHS;
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        up[c] = cadd(up[c], w[c]);
-        const cx<float> c2 = mulc<Pj::b2 ^ f>(w[c]);
-        const cx<float> c3 = mulc<Pj::b3 ^ f>(w[c]);
-        if (to2) l2[c] = cadd(l2[c], c2);
-        else l3[c] = cadd(l3[c], c3);
+        for (int k = 0; k < 3; k++) {
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(pf + k * a.cs));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(pb + k * a.cs));
+        }
+        if (item) {
+            const char *blk = a.gauge + (size_t)((dir == 0 ? a.pt : 1 - a.pt) * 4 + MU) * a.link_block_bytes;
+            const size_t ls = (size_t)(dir == 0 ? co.h : b);
+            const size_t stride = (size_t)a.g.stride;
+            if constexpr (RECON == 18) {
+                const float2 *p0 = reinterpret_cast<const float2 *>(blk) + ls + (size_t)(dir == 0 ? 3 * c : c) * stride;
+                const size_t step = (dir == 0 ? 1 : 3) * stride;
+#pragma unroll
+                for (int ci = 0; ci < 3; ci++) asm volatile("prefetch.global.L1 [%0];" ::"l"(p0 + ci * step));
+            } else {
+                const float4 *pl = reinterpret_cast<const float4 *>(blk) + ls;
+#pragma unroll
+                for (int k = 0; k < 3; k++) asm volatile("prefetch.global.L1 [%0];" ::"l"(pl + k * stride));
+            }
+        }
     }
+
+    // The A row to TMEM and the B rows to shared memory; returns the D row
+    // scale (half + norm).
+    template <int MU>
+    __device__ __forceinline__ float prep(const Raw &raw, uint32_t arow) const {
+        uint32_t f0[3], f1[3], b0[3], b1[3];
+        project_packed<FMT, MU, ISIGN>(raw.qf, f0, f1);   // forward hop: 1 - isign gamma_mu
+        project_packed<FMT, MU, -ISIGN>(raw.qb, b0, b1);  // backward hop: 1 + isign gamma_mu
+        float m = 1.f;
+        if constexpr (FMT == kFmtF16N) {
+            // one scale per A row: the larger of the two neighbour norms
+            m = fmaxf(raw.nf, raw.nb);
+            const float inv = m > 0.f ? 1.f / m : 0.f;
+            const uint32_t sf = Pk<FMT>::pack(raw.nf * inv, raw.nf * inv);
+            const uint32_t sb = Pk<FMT>::pack(raw.nb * inv, raw.nb * inv);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                f0[k] = Pk<FMT>::mul2(f0[k], sf);
+                f1[k] = Pk<FMT>::mul2(f1[k], sf);
+                b0[k] = Pk<FMT>::mul2(b0[k], sb);
+                b1[k] = Pk<FMT>::mul2(b1[k], sb);
+            }
+        }
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+                arow),
+            "r"(f0[0]), "r"(f0[1]), "r"(f0[2]), "r"(0u), "r"(f1[0]), "r"(f1[1]), "r"(f1[2]), "r"(0u), "r"(b0[0]),
+            "r"(b0[1]), "r"(b0[2]), "r"(0u), "r"(b1[0]), "r"(b1[1]), "r"(b1[2]), "r"(0u));
+        if (item) {
+            float mr[3], mi[3];
+            link_row<RECON>(raw.l, dir, c, mr, mi);
+            const uint4 rr = make_uint4(Pk<FMT>::pack(mr[0], -mi[0]), Pk<FMT>::pack(mr[1], -mi[1]),
+                                        Pk<FMT>::pack(mr[2], -mi[2]), 0u);
+            const uint4 ri = make_uint4(Pk<FMT>::pack(mi[0], mr[0]), Pk<FMT>::pack(mi[1], mr[1]),
+                                        Pk<FMT>::pack(mi[2], mr[2]), 0u);
+            const uint32_t ng = dir == 0 ? 0u : 0x80008000u;  // the difference rows negate the backward block
+            const uint4 nr = make_uint4(rr.x ^ ng, rr.y ^ ng, rr.z ^ ng, 0u);
+            const uint4 ni = make_uint4(ri.x ^ ng, ri.y ^ ng, ri.z ^ ng, 0u);
+            const int base = p * 24 + 2 * c;
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int kg = dir * 2 + hh;
+                *reinterpret_cast<uint4 *>(B + core_off(base + 6 * hh, kg)) = rr;
+                *reinterpret_cast<uint4 *>(B + core_off(base + 6 * hh + 1, kg)) = ri;
+                *reinterpret_cast<uint4 *>(B + core_off(base + 12 + 6 * hh, kg)) = nr;
+                *reinterpret_cast<uint4 *>(B + core_off(base + 12 + 6 * hh + 1, kg)) = ni;
+            }
+        }
+        return m;
+    }
+
+    // Fold one direction's sums and differences (24 values: sum h0, sum h1,
+    // diff h0, diff h1, 3 complex each) into the output spinor.
+    template <int MU>
+    __device__ __forceinline__ void fold(const uint32_t (&d)[24], float m, cx<float> (&o)[4][3]) const {
+        using P = Proj<MU>;
+        constexpr int f = ISIGN > 0 ? 0 : 1;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const cx<float> s0 = {__uint_as_float(d[2 * k]) * m, __uint_as_float(d[2 * k + 1]) * m};
+            const cx<float> s1 = {__uint_as_float(d[6 + 2 * k]) * m, __uint_as_float(d[7 + 2 * k]) * m};
+            const cx<float> d0 = {__uint_as_float(d[12 + 2 * k]) * m, __uint_as_float(d[13 + 2 * k]) * m};
+            const cx<float> d1 = {__uint_as_float(d[18 + 2 * k]) * m, __uint_as_float(d[19 + 2 * k]) * m};
+            o[0][k] = cadd(o[0][k], s0);
+            o[1][k] = cadd(o[1][k], s1);
+            o[2][k] = cadd(o[2][k], mulc<P::b2 ^ f>(P::k2 == 0 ? d0 : d1));
+            o[3][k] = cadd(o[3][k], mulc<P::b3 ^ f>(P::k3 == 0 ? d0 : d1));
+        }
+    }
+
+    // This row's 24 columns of D (its site's block).
+    __device__ __forceinline__ void read_d(uint32_t tmem, uint32_t (&d)[24]) const {
+        const uint32_t lane = (uint32_t)(32 * w) << 16;
+        if constexpr (NRHS >= 32) {
+            const uint32_t col = (uint32_t)(p * 24);  // one site per warp
+            tmem_ld<16>(tmem + lane + col, d);
+            tmem_ld<8>(tmem + lane + col + 16, d + 16);
+        } else {
+            // two sites per warp: read both blocks, keep this lane's
+            const uint32_t col = (uint32_t)((32 * w / NRHS) * 24);
+            uint32_t e[48];
+            tmem_ld<16>(tmem + lane + col, e);
+            tmem_ld<16>(tmem + lane + col + 16, e + 16);
+            tmem_ld<16>(tmem + lane + col + 32, e + 32);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const bool hi = (t & 31) >= NRHS;
+#pragma unroll
+            for (int k = 0; k < 24; k++) d[k] = hi ? e[24 + k] : e[k];
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    }
+};
+
+__device__ __forceinline__ bool wait_parity(uint32_t mbar, uint32_t parity) {
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 20) && !done; it++) {
+        asm volatile(
+            "{\n.reg .pred pw;\nmbarrier.try_wait.parity.shared::cta.b64 pw, [%1], %2;\nselp.u32 %0, 1, 0, pw;\n}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+    }
+    return done != 0;
 }
 
-template <int FMT, int RECON, int ISIGN, int NRHS, int HR>
-__global__ void __launch_bounds__(128) dslash_tc_kernel(const TcArgs a) {
-    using S = TcShape<NRHS, HR>;
-    extern __shared__ __align__(1024) unsigned char smem[];
+template <int FMT, int RECON, int ISIGN, int NRHS>
+__global__ void __launch_bounds__(128, 512 / TcShape<NRHS>::COLS) dslash_tc_kernel(const __grid_constant__ TcArgs a) {
+    using S = TcShape<NRHS>;
+    using Cta = TcCta<FMT, RECON, ISIGN, NRHS>;
+    __shared__ __align__(128) unsigned char sB[S::B_BYTES];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tbase;
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int p = t / (2 * NRHS), loc = t % (2 * NRHS), r = loc / 2, s = loc % 2, j = loc;
-    const int h = blockIdx.x * S::P + p;
-    const bool active = h < a.g.Vh;
-    unsigned char *Abuf = smem;
-    unsigned char *Bbuf = smem + HR * S::A_BYTES;
-    // zero the operand buffers once (the k = 8..15 core matrices stay zero)
-    for (int i = t; i < S::SMEM / 16; i += 128) reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
-    if (w == 0) {
+    Cta cta(a, sB);
+    const int t = threadIdx.x;
+    // rows and k-groups that no link-row thread writes stay zero
+    for (int i = t; i < S::B_BYTES / 16; i += 128) reinterpret_cast<uint4 *>(sB)[i] = make_uint4(0, 0, 0, 0);
+    if (cta.w == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tbase)),
                      "r"(S::COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -179,126 +482,123 @@ __global__ void __launch_bounds__(128) dslash_tc_kernel(const TcArgs a) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    Nbr n;
-    if (active) neighbours<4>(a.g, active ? h : 0, a.pt, n);
-    asm volatile("tcgen05.fence::before_thread_sync;");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tbase;
-    constexpr uint32_t idesc = (1u << 4) | ((FMT == kFmtBF16 ? 1u : 0u) << 7) | ((FMT == kFmtBF16 ? 1u : 0u) << 10) |
-                               ((uint32_t)(S::N >> 3) << 17) | ((128u >> 4) << 24);
-    cx<float> up[3], l2[3], l3[3];
+    const uint32_t mb = smem_u32(&mbar);
+    constexpr uint32_t fmt = FMT == kFmtBF16 ? 1u : 0u;
+    constexpr uint32_t idesc =
+        (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(S::N >> 3) << 17) | ((128u >> 4) << 24);
+    const uint64_t bdesc0 = smem_desc(smem_u32(sB)), bdesc1 = smem_desc(smem_u32(sB) + 256);
+    const uint32_t arow = tmem + ((uint32_t)(32 * cta.w) << 16) + S::ACOL;
+
+    // grid-stride walk: at any time the CTAs work on one contiguous band of
+    // sites, so a spinor's eight uses fall close together in time (L2 reuse)
+    int tile = blockIdx.x;
+    int h = tile * S::P + cta.p;
+    bool act = tile < a.ntiles && h < a.g.Vh;
+    Co co = coords(a, act ? h : 0);
+    Raw raw;
+    cta.template load<0>(co, act, raw);
+    cta.template prefetch<1>(co, act);
+    uint32_t phase = 0;
+    bool bad = false;
+
+    while (tile < a.ntiles) {
+        const int ntile = tile + gridDim.x;
+        const int nh = ntile * S::P + cta.p;
+        const bool nact = ntile < a.ntiles && nh < a.g.Vh;
+        Co nco = co;
+        cx<float> o[4][3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) up[c] = l2[c] = l3[c] = {0.f, 0.f};
-    float nrm_scale[8];
-    bool ok = true;
+        for (int s = 0; s < 4; s++)
 #pragma unroll
-    for (int round = 0; round < 8 / HR; round++) {
-        // ---- operands for HR hops
-#pragma unroll
-        for (int q = 0; q < HR; q++) {
-            const int hop = round * HR + q;
-#define GBDS_PREP(H) \
-    if (hop == H) tc_prepare<FMT, RECON, ISIGN, NRHS, H>(a, active, h, r, s, p, j, n, Abuf + q * S::A_BYTES, Bbuf + q * S::B_BYTES)
-            GBDS_PREP(0); GBDS_PREP(1); GBDS_PREP(2); GBDS_PREP(3); GBDS_PREP(4); GBDS_PREP(5); GBDS_PREP(6); GBDS_PREP(7);
-#undef GBDS_PREP
-        }
-        if constexpr (FMT == kFmtF16N) {
-            // the tensor core multiplies normalised halves; scale D rows by the
-            // neighbour spinor's norm afterwards
-#pragma unroll
-            for (int q = 0; q < HR; q++) {
-                const int hop = round * HR + q, mu = hop / 2;
-                float v = 0.f;
-                if (active) {
-                    const int nb = (hop % 2 == 0) ? n.f[mu] : n.b[mu];
-                    v = __ldg(Sio<kFmtF16N>::norms(a.psi, a.cs) + (size_t)nb * NRHS + r);
-                }
-                nrm_scale[q] = v;
-            }
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (t == 0) {
-#pragma unroll
-            for (int q = 0; q < HR; q++) {
-                const uint64_t ad = smem_desc(smem_u32(Abuf + q * S::A_BYTES));
-                const uint64_t bd = smem_desc(smem_u32(Bbuf + q * S::B_BYTES));
-                asm volatile("{\n.reg .pred pd;\nsetp.ne.b32 pd, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pd;\n}" ::"r"(
-                                 tmem + q * S::N),
-                             "l"(ad), "l"(bd), "r"(idesc), "r"(0));
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar)));
-        }
-        // bounded wait for this round's MMAs; the whole CTA agrees on the outcome
-        uint32_t done = 0;
-        for (int it = 0; it < (1 << 20) && !done; it++) {
-            asm volatile("{\n.reg .pred pw;\nmbarrier.try_wait.parity.shared::cta.b64 pw, [%1], %2;\nselp.u32 %0, 1, 0, pw;\n}"
-                         : "=r"(done)
-                         : "r"(smem_u32(&mbar)), "r"(round & 1));
-        }
-        if (!__syncthreads_and(done)) {
-            ok = false;
-            if (t == 0) atomicExch(a.err, 1);
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        // ---- read back and reconstruct
-        const int pw = (32 * w) / (2 * NRHS);  // site block of this warp's rows
-#pragma unroll
-        for (int q = 0; q < HR; q++) {
-            uint32_t d[8];
-            const uint32_t taddr = tmem + ((uint32_t)(32 * w) << 16) + q * S::N + pw * 8;
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                         : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7])
-                         : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
-            const float sc = FMT == kFmtF16N ? nrm_scale[q] : 1.f;
-            cx<float> wv[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) wv[c] = {__uint_as_float(d[2 * c]) * sc, __uint_as_float(d[2 * c + 1]) * sc};
-            const int hop = round * HR + q;
-#define GBDS_REC(H) if (hop == H) tc_reconstruct<ISIGN, H>(s, wv, up, l2, l3)
-            GBDS_REC(0); GBDS_REC(1); GBDS_REC(2); GBDS_REC(3); GBDS_REC(4); GBDS_REC(5); GBDS_REC(6); GBDS_REC(7);
-#undef GBDS_REC
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();  // everyone has read TMEM and the operands before the next round
-        asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int k = 0; k < 3; k++) o[s][k] = {0.f, 0.f};
+
+#define GBDS_TC_ROUND(MU, NEXT_LOAD, NEXT_PREFETCH)                                                                            \
+    {                                                                                                             \
+        const float m = cta.template prep<MU>(raw, arow);                                                         \
+        NEXT_LOAD;                                                                                                \
+        NEXT_PREFETCH;                                                                                            \
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");                                              \
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");                                              \
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");                                          \
+        __syncthreads();                                                                                          \
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");                                           \
+        /* one thread issues the MMAs and waits for them; the others wait at */                                 \
+        /* the barrier, which costs them no issue slots */                                                        \
+        bool timed_out = false;                                                                                   \
+        if (t == 0) {                                                                                             \
+            asm volatile("{\n.reg .pred pd;\nsetp.ne.b32 pd, %4, 0;\n"                                            \
+                         "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, pd;\n}" ::"r"(tmem),             \
+                         "r"(tmem + S::ACOL), "l"(bdesc0), "r"(idesc), "r"(0));                                   \
+            asm volatile("{\n.reg .pred pd;\nsetp.ne.b32 pd, %4, 0;\n"                                            \
+                         "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, pd;\n}" ::"r"(tmem),             \
+                         "r"(tmem + S::ACOL + 8), "l"(bdesc1), "r"(idesc), "r"(1));                               \
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)  \
+                         : "memory");                                                                             \
+            timed_out = !wait_parity(mb, phase);                                                                  \
+        }                                                                                                         \
+        phase ^= 1u;                                                                                              \
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");                                          \
+        bad = __syncthreads_or(timed_out);                                                                        \
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");                                           \
+        if (bad) break;                                                                                           \
+        uint32_t d[24];                                                                                           \
+        cta.read_d(tmem, d);                                                                                      \
+        cta.template fold<MU>(d, m, o);                                                                           \
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");                                          \
     }
-    // ---- combine the spin halves of each rhs and store
-    if (ok) {
-        cx<float> out[4][3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const cx<float> o_up = {__shfl_xor_sync(0xffffffffu, up[c].r, 1), __shfl_xor_sync(0xffffffffu, up[c].i, 1)};
-            const cx<float> o_l2 = {__shfl_xor_sync(0xffffffffu, l2[c].r, 1), __shfl_xor_sync(0xffffffffu, l2[c].i, 1)};
-            const cx<float> o_l3 = {__shfl_xor_sync(0xffffffffu, l3[c].r, 1), __shfl_xor_sync(0xffffffffu, l3[c].i, 1)};
-            out[0][c] = s == 0 ? up[c] : o_up;
-            out[1][c] = s == 0 ? o_up : up[c];
-            out[2][c] = cadd(l2[c], o_l2);
-            out[3][c] = cadd(l3[c], o_l3);
-        }
-        if (active && s == 0) Sio<FMT>::store(a.res, a.cs, (size_t)h * NRHS + r, out);
+
+        GBDS_TC_ROUND(0, cta.template load<1>(co, act, raw), cta.template prefetch<2>(co, act))
+        GBDS_TC_ROUND(1, cta.template load<2>(co, act, raw), cta.template prefetch<3>(co, act))
+        GBDS_TC_ROUND(2, cta.template load<3>(co, act, raw),
+                      (nco = coords(a, nact ? nh : 0), cta.template prefetch<0>(nco, nact)))
+        GBDS_TC_ROUND(3, cta.template load<0>(nco, nact, raw), cta.template prefetch<1>(nco, nact))
+#undef GBDS_TC_ROUND
+
+        if (act) Sio<FMT>::store(a.res, a.cs, (size_t)h * NRHS + cta.r, o);
+        tile = ntile;
+        h = nh;
+        act = nact;
+        co = nco;
     }
-    asm volatile("tcgen05.fence::before_thread_sync;");
+    if (bad && t == 0) {
+        atomicExch(a.err, 1);
+        // the MMAs whose wait ran out may still be in flight: wait once more
+        // (bounded) before their columns are freed
+        wait_parity(mb, phase ^ 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::COLS));
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (cta.w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::COLS));
 }
 
-template <int FMT, int RECON, int ISIGN, int NRHS, int HR>
-cudaError_t launch_tc_t(const TcArgs &a, cudaStream_t st) {
-    using S = TcShape<NRHS, HR>;
-    auto k = dslash_tc_kernel<FMT, RECON, ISIGN, NRHS, HR>;
-    // at most 4 CTAs per SM: 4 x S::COLS <= 512 TMEM columns
-    const int smem = S::SMEM < 48 * 1024 ? 48 * 1024 : S::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+template <int FMT, int RECON, int ISIGN, int NRHS>
+cudaError_t launch_tc_t(TcArgs a, cudaStream_t st) {
+    using S = TcShape<NRHS>;
+    auto k = dslash_tc_kernel<FMT, RECON, ISIGN, NRHS>;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k);
     if (e != cudaSuccess) return e;
-    const unsigned grid = (unsigned)((a.g.Vh + S::P - 1) / S::P);
-    k<<<grid, 128, smem, st>>>(a);
+    // resident CTAs per SM: 64K registers (allocated per warp in steps of
+    // 256), 228 KB of shared memory (1 KB reserved per CTA), 2048 threads,
+    // and the 512 TMEM columns
+    const int regs = ((fa.numRegs * 32 + 255) / 256) * 256 * 4;
+    int occ = 65536 / (regs > 0 ? regs : 1);
+    const int by_smem = (228 * 1024) / ((int)fa.sharedSizeBytes + 1024);
+    occ = occ < by_smem ? occ : by_smem;
+    occ = occ < 16 ? occ : 16;
+    occ = occ < 512 / S::COLS ? occ : 512 / S::COLS;
+    occ = occ < 1 ? 1 : occ;
+    a.ntiles = (a.g.Vh + S::P - 1) / S::P;
+    const int grid = a.ntiles < sms * occ ? a.ntiles : sms * occ;
+    k<<<grid, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -310,15 +610,19 @@ cudaError_t launch_gen_tc(int fmt, const Geom &g, int recon, int nrhs, const voi
                           int isign, int cb, int *err, cudaStream_t st) {
     TcArgs a;
     a.g = g;
+    a.dx = make_fastdiv((uint32_t)g.Lxh);
+    a.dy = make_fastdiv((uint32_t)g.L[1]);
+    a.dz = make_fastdiv((uint32_t)g.L[2]);
     a.psi = static_cast<const char *>(psi);
     a.res = static_cast<char *>(res);
     a.gauge = static_cast<const char *>(gauge);
     a.link_block_bytes = (size_t)recon * 4 * g.stride;
     a.cs = (size_t)g.stride * nrhs;
     a.pt = 1 - cb;
+    a.ntiles = 0;
     a.err = err;
     cudaError_t e = cudaErrorInvalidValue;
-#define GBDS_TC(F, R, S, N) e = launch_tc_t<F, R, S, N, (N == 32 ? 8 : 4)>(a, st)
+#define GBDS_TC(F, R, S, N) e = launch_tc_t<F, R, S, N>(a, st)
 #define GBDS_TC_N(F, R, S) do { if (nrhs == 32) GBDS_TC(F, R, S, 32); else if (nrhs == 16) GBDS_TC(F, R, S, 16); } while (0)
 #define GBDS_TC_S(F, R) do { if (isign > 0) GBDS_TC_N(F, R, 1); else GBDS_TC_N(F, R, -1); } while (0)
 #define GBDS_TC_R(F) do { if (recon == 18) GBDS_TC_S(F, 18); else GBDS_TC_S(F, 12); } while (0)

@@ -69,18 +69,20 @@ def test_multi_rhs_bytes_accounting():
 # spinor and the link enter the MMA rounded to the 16-bit operand type (one
 # more rounding of each, FP32 accumulation), well inside the same per-site
 # bounds.
+# (8, 4, 6, 4): one tile per CTA; (16, 8, 8, 16): every persistent CTA walks
+# several tiles, so the loads of the next tile overlap the last MMA of this one.
+@pytest.mark.parametrize("dims", [(8, 4, 6, 4), (16, 8, 8, 16)])
 @pytest.mark.parametrize("fmt", ["bf16", "f16"])
 @pytest.mark.parametrize("nrhs", [16, 32])
-def test_tensor_core_multi_rhs_matches_oracle(nrhs, fmt):
+def test_tensor_core_multi_rhs_matches_oracle(nrhs, fmt, dims):
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
-    dims = (8, 4, 6, 4)
     V = O.volume(dims)
     lol = O.layout_table(O.LAYOUT_CB2, dims)
     rng = np.random.default_rng(100 + nrhs)
     u = O.random_gauge(rng, V)
     psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
-    for recon in (18, 12):
+    for recon in ((18, 12) if V < 4096 else (18,)):
         op = DslashOperator(dims, nd=4, prec=32, recon=recon, nrhs=nrhs, spinor_format=fmt)
         op.set_tensor_cores(True)
         gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
@@ -108,3 +110,31 @@ def test_tensor_cores_need_16bit_and_16_or_32_rhs():
         with pytest.raises(_lib.GbdsError):
             op.set_tensor_cores(True)
         op.close()
+
+
+@pytest.mark.parametrize("fmt", ["bf16", "f16"])
+def test_autotune_chooses_between_cuda_and_tensor_cores(fmt):
+    """The autotuner times both kernels for a 16-bit, 32-rhs operator; the
+    pick (cached) gives the same answer as the oracle."""
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims, nrhs = (8, 8, 8, 8), 32
+    V = O.volume(dims)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    rng = np.random.default_rng(9)
+    u = O.random_gauge(rng, V)
+    psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
+    op = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
+    gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
+    src = op.pack_spinor(torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda(), 0)
+    op.autotune(gauge, src, op.new_spinor())
+    out = op.apply(gauge, src, 1, 0)
+    op.check()
+    res = torch.zeros(nrhs * V * 24, dtype=torch.float32, device="cuda")
+    op.unpack_spinor(out, 1, res)
+    got = res.cpu().numpy().reshape(nrhs, V, 24)
+    ts = O.target_sites(4, dims, lol, 0)
+    for r in range(0, nrhs, 7):
+        ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), 1, 0)
+        assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt]
+    op.close()
