@@ -622,23 +622,30 @@ def run_gb300(args):
     variants = {}
     if not args.no_variants:
         vsteps = max(20, min(args.steps, 200))
-        f32 = (u, psi)
-        variants["f32_recon12"] = device_variant(DIMS, 4, 32, 12, vsteps, 5, torch, fields=f32)
-        del f32
-        u64, psi64 = u.double(), psi.double()
-        del u, psi
+        want = set(args.variants.split(","))
+        run = lambda name: "all" in want or name in want  # noqa: E731
+        if run("recon12"):
+            variants["f32_recon12"] = device_variant(DIMS, 4, 32, 12, vsteps, 5, torch, fields=(u, psi))
+        if run("f64"):
+            u64, psi64 = u.double(), psi.double()
+            del u, psi
+            torch.cuda.empty_cache()
+            variants["f64_recon18"] = device_variant(DIMS, 4, 64, 18, vsteps, 5, torch, fields=(u64, psi64))
+            variants["f64_recon12"] = device_variant(DIMS, 4, 64, 12, vsteps, 5, torch, fields=(u64, psi64))
+            del u64, psi64
+        else:
+            del u, psi
         torch.cuda.empty_cache()
-        variants["f64_recon18"] = device_variant(DIMS, 4, 64, 18, vsteps, 5, torch, fields=(u64, psi64))
-        variants["f64_recon12"] = device_variant(DIMS, 4, 64, 12, vsteps, 5, torch, fields=(u64, psi64))
-        del u64, psi64
-        torch.cuda.empty_cache()
-        variants["3d_24x24x24x48_f32_recon18"] = device_variant(DIMS_3D, 3, 32, 18, vsteps, 5, torch)
-        variants["3d_24x24x24x48_f32_recon12"] = device_variant(DIMS_3D, 3, 32, 12, vsteps, 5, torch)
+        if run("3d"):
+            variants["3d_24x24x24x48_f32_recon18"] = device_variant(DIMS_3D, 3, 32, 18, vsteps, 5, torch)
+            variants["3d_24x24x24x48_f32_recon12"] = device_variant(DIMS_3D, 3, 32, 12, vsteps, 5, torch)
         for v in variants.values():
             v["roofline_frac"] = v["gbs"] / peak
-        variants["multi_rhs_24x24x24x48"] = multi_rhs_variants(torch, vsteps, peak)
-        torch.cuda.empty_cache()
-        variants["uneven_batch"] = uneven_batch(torch, peak)
+        if run("multi_rhs"):
+            variants["multi_rhs_24x24x24x48"] = multi_rhs_variants(torch, vsteps, peak)
+            torch.cuda.empty_cache()
+        if run("uneven_batch"):
+            variants["uneven_batch"] = uneven_batch(torch, peak)
 
     solver = None
     if not args.no_solver:
@@ -681,6 +688,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true")
+    ap.add_argument("--variants", default="all",
+                    help="comma list of variant sections: recon12, f64, 3d, multi_rhs, uneven_batch (default all)")
     ap.add_argument("--tuning", default=None,
                     help="block,variant of the headline kernel instead of autotuning (for profiling runs)")
     ap.add_argument("--dims", default=None,
