@@ -138,3 +138,35 @@ def test_autotune_chooses_between_cuda_and_tensor_cores(fmt):
         ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), 1, 0)
         assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt]
     op.close()
+
+
+# Smallest and uneven shapes for the tensor-core kernel: a 2^4 lattice (two
+# tiles with 32 rhs), Lx = 2 (half extent 1: the division-free path of the
+# coordinate decomposition) and extents of different lengths in every
+# direction.
+@pytest.mark.parametrize("dims", [(2, 2, 2, 2), (2, 4, 6, 2), (6, 2, 4, 10)])
+@pytest.mark.parametrize("nrhs", [16, 32])
+def test_tensor_core_edge_lattices(dims, nrhs):
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    fmt = "bf16"
+    V = O.volume(dims)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    rng = np.random.default_rng(sum(dims) + nrhs)
+    u = O.random_gauge(rng, V)
+    psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
+    op = DslashOperator(dims, nd=4, prec=32, recon=12, nrhs=nrhs, spinor_format=fmt)
+    op.set_tensor_cores(True)
+    gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
+    packed = torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda()
+    for isign, cb in ((1, 1), (-1, 0)):
+        out = op.apply(gauge, op.pack_spinor(packed, cb), isign, cb)
+        op.check()
+        res = torch.zeros(nrhs * V * 24, dtype=torch.float32, device="cuda")
+        op.unpack_spinor(out, 1 - cb, res)
+        got = res.cpu().numpy().reshape(nrhs, V, 24)
+        ts = O.target_sites(4, dims, lol, cb)
+        for r in range(nrhs):
+            ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
+            assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt], (dims, isign, cb, r)
+    op.close()
