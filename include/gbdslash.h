@@ -111,6 +111,11 @@ int gbds_op_nrhs(gbds_op op);
  * MMAs ran out (it then wrote nothing for those sites). */
 int gbds_op_set_tensor_cores(gbds_op op, int on);
 int gbds_op_check(gbds_op op);
+/* Diagnostic: runs the tensor-core kernel's bounded mbarrier wait, with
+ * `polls` polls, on a barrier that nothing completes, and returns
+ * GBDS_SUCCESS when the wait gave up and reported it (the context stays
+ * usable).  No reference counterpart. */
+int gbds_tc_wait_selftest(int polls);
 
 /* Caller site layout for pack/unpack: site_table[i] = caller linear index of
  * internal site i (i = p*Vh + h, internal order above), n = V entries, a

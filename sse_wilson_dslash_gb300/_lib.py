@@ -68,6 +68,7 @@ def core() -> ctypes.CDLL:
     L.gbds_op_nrhs.argtypes = [vp]
     L.gbds_op_set_tensor_cores.argtypes = [vp, i]
     L.gbds_op_check.argtypes = [vp]
+    L.gbds_tc_wait_selftest.argtypes = [i]
     L.gbds_op_destroy.argtypes = [vp]
     L.gbds_op_set_layout.argtypes = [vp, c_int_p, i]
     L.gbds_op_is_canonical.argtypes = [vp]

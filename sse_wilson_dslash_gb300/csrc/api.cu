@@ -200,6 +200,20 @@ extern "C" int gbds_op_check(gbds_op op) {
     return GBDS_SUCCESS;
 }
 
+extern "C" int gbds_tc_wait_selftest(int polls) {
+    if (polls <= 0) return set_error(GBDS_ERROR_INVALID_VALUE, "polls must be positive");
+    int *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(int));
+    if (e != cudaSuccess) return cuda_error(e, "gbds_tc_wait_selftest");
+    int flag = -1;
+    e = cudaMemset(d, 0xff, sizeof(int));
+    if (e == cudaSuccess) e = launch_tc_wait_selftest(polls, d, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_tc_wait_selftest");
+    return flag == 1 ? GBDS_SUCCESS : set_error(GBDS_ERROR_CUDA, "the bounded wait did not report its time-out");
+}
+
 extern "C" size_t gbds_op_gauge_bytes(gbds_op op) { return op ? gauge_bytes(op->g, op->prec, op->recon) : 0; }
 
 extern "C" int gbds_op_geometry(gbds_op op, int *volume, int *volume_cb, int *stride) {

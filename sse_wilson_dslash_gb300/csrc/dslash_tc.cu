@@ -450,9 +450,11 @@ struct TcCta {
     }
 };
 
-__device__ __forceinline__ bool wait_parity(uint32_t mbar, uint32_t parity) {
+// Bounded wait for the phase of `parity` of an mbarrier: false if it has not
+// completed after `polls` polls.
+__device__ __forceinline__ bool wait_parity(uint32_t mbar, uint32_t parity, int polls = 1 << 20) {
     uint32_t done = 0;
-    for (int it = 0; it < (1 << 20) && !done; it++) {
+    for (int it = 0; it < polls && !done; it++) {
         asm volatile(
             "{\n.reg .pred pw;\nmbarrier.try_wait.parity.shared::cta.b64 pw, [%1], %2;\nselp.u32 %0, 1, 0, pw;\n}"
             : "=r"(done)
@@ -602,7 +604,26 @@ cudaError_t launch_tc_t(TcArgs a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// A wait that nothing completes: an mbarrier that no thread or copy arrives
+// on.  flag = 1 when the bounded wait gave up (as the Dslash kernel's waits
+// do), 0 if it (wrongly) saw the phase complete.
+__global__ void tc_wait_selftest_kernel(int polls, int *flag) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool done = wait_parity(smem_u32(&bar), 0u, polls);
+    if (threadIdx.x == 0) *flag = done ? 0 : 1;
+}
+
 }  // namespace
+
+cudaError_t launch_tc_wait_selftest(int polls, int *flag, cudaStream_t st) {
+    tc_wait_selftest_kernel<<<1, 32, 0, st>>>(polls, flag);
+    return cudaGetLastError();
+}
 
 // fmt: kFmtBF16 or kFmtF16N; nrhs: 16 or 32; err: device int set to 1 if a
 // wait on the tensor-core completion timed out.

@@ -74,6 +74,9 @@ inline int gen_spinor_bytes(int fmt) { return fmt == 0 ? 96 : (fmt == 1 ? 48 : 5
 // converted to the 16-bit operand type; err set to 1 on a timed-out wait.
 cudaError_t launch_gen_tc(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,
                           int isign, int cb, int *err, cudaStream_t st);
+// The tensor-core kernel's bounded mbarrier wait on a barrier nothing
+// completes; flag = 1 when the wait gave up.
+cudaError_t launch_tc_wait_selftest(int polls, int *flag, cudaStream_t st);
 // nrhs 1, 16-bit spinors (fmt 1 / 2) with FP16 links: gauge is the FP32
 // internal gauge converted by convert_links_f16 (recon * 2 bytes per link
 // per site-stride).

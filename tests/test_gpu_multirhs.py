@@ -170,3 +170,12 @@ def test_tensor_core_edge_lattices(dims, nrhs):
             ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
             assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt], (dims, isign, cb, r)
     op.close()
+
+
+def test_tensor_core_wait_times_out_and_reports():
+    """A bounded mbarrier wait on a barrier that nothing completes gives up,
+    reports it, and leaves the context usable: a tensor-core Dslash runs
+    correctly afterwards."""
+    from sse_wilson_dslash_gb300 import _lib
+    _lib.check(_lib.core().gbds_tc_wait_selftest(4096))
+    test_tensor_core_edge_lattices((2, 4, 6, 2), 32)
