@@ -117,6 +117,28 @@ __device__ __forceinline__ void reconstruct_row2(cx<T> (&U)[3][3]) {
 
 template <typename T> struct Field;
 
+// The single right-hand-side operator reads every link once per
+// application: it loads them without allocating in L1 and marks their L2
+// lines first for eviction, so that L2 keeps the source spinors, which are
+// read by eight neighbours.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float2 ld_once(const float2 *p, uint64_t pol) {
+    float2 v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float4 ld_once(const float4 *p, uint64_t pol) {
+    float4 v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(p), "l"(pol));
+    return v;
+}
+
 template <>
 struct Field<float> {
     static constexpr int SPINOR_VECS = 6;  // float4
@@ -145,21 +167,25 @@ struct Field<float> {
     }
     // Link block base: vector elements per link for a recon.
     static constexpr int link_vecs(int recon) { return recon == 18 ? 9 : 3; }
-    template <int RECON>
+    // ONCE: the caller reads each link once per launch (the single
+    // right-hand-side operator); the hints are measured to cost the kernels
+    // that read a link several times (several rhs, batches).
+    template <int RECON, bool ONCE = false>
     __device__ __forceinline__ static void load_link(const void *__restrict__ base, int stride, int h,
                                                      cx<float> (&U)[3][3]) {
+        const uint64_t pol = ONCE ? l2_evict_first_policy() : 0;
         if constexpr (RECON == 18) {
             const float2 *p = static_cast<const float2 *>(base);
 #pragma unroll
             for (int k = 0; k < 9; k++) {
-                float2 q = __ldg(p + k * stride + h);
+                float2 q = ONCE ? ld_once(p + k * stride + h, pol) : __ldg(p + k * stride + h);
                 U[k / 3][k % 3] = {q.x, q.y};
             }
         } else {
             const float4 *p = static_cast<const float4 *>(base);
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                float4 q = __ldg(p + k * stride + h);
+                float4 q = ONCE ? ld_once(p + k * stride + h, pol) : __ldg(p + k * stride + h);
                 U[(2 * k) / 3][(2 * k) % 3] = {q.x, q.y};
                 U[(2 * k + 1) / 3][(2 * k + 1) % 3] = {q.z, q.w};
             }
@@ -185,7 +211,7 @@ struct Field<double> {
         for (int k = 0; k < 12; k++) __stcs(p + k * stride + h, make_double2(s[k / 3][k % 3].r, s[k / 3][k % 3].i));
     }
     static constexpr int link_vecs(int recon) { return recon == 18 ? 9 : 6; }
-    template <int RECON>
+    template <int RECON, bool ONCE = false>
     __device__ __forceinline__ static void load_link(const void *__restrict__ base, int stride, int h,
                                                      cx<double> (&U)[3][3]) {
         const double2 *p = static_cast<const double2 *>(base);
@@ -281,13 +307,13 @@ __device__ __forceinline__ void hop_pair(const DslashArgs<T> &a, int h, const Nb
     cx<T> s[4][3], hs[2][3], w[2][3], U[3][3];
     // forward: U_mu(x) (1 - isign gamma_mu) psi(x + mu)
     F::load_spinor(a.psi, a.g.stride, n.f[MU], s);
-    F::template load_link<RECON>(a.gauge + (size_t)(a.pt * ND + MU) * a.link_block_bytes, a.g.stride, h, U);
+    F::template load_link<RECON, true>(a.gauge + (size_t)(a.pt * ND + MU) * a.link_block_bytes, a.g.stride, h, U);
     project<MU, ISIGN>(s, hs);
     su3_mul<false>(U, hs, w);
     reconstruct<MU, ISIGN>(acc, w);
     // backward: U_mu(x - mu)^dagger (1 + isign gamma_mu) psi(x - mu)
     F::load_spinor(a.psi, a.g.stride, n.b[MU], s);
-    F::template load_link<RECON>(a.gauge + (size_t)(ps * ND + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
+    F::template load_link<RECON, true>(a.gauge + (size_t)(ps * ND + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
     project<MU, -ISIGN>(s, hs);
     su3_mul<true>(U, hs, w);
     reconstruct<MU, -ISIGN>(acc, w);
