@@ -307,6 +307,20 @@ int gbds_solver_solve(gbds_solver s, const double *b_packed, double *x_packed, g
 int gbds_solver_solve_normal(gbds_solver s, const double *c_packed, double *x_packed, gbds_solver_stats *stats,
                              void *stream);
 
+/* Batched solve (no reference counterpart): nrhs (2, 4, 8, 16 or 32)
+ * independent systems M x_q = b_q on one gauge field.  The inner FP32 CGs of
+ * all right-hand sides advance together on the multi-RHS operator (each link
+ * load serves every right-hand side), each with its own scalars and stopping
+ * point; the FP64 defect correction runs per right-hand side.  params as for
+ * gbds_solver_create with inner_prec 32.  b_packed, x_packed: FP64 device
+ * arrays [nrhs][V][4][3][2] (cb2 order, even sites used / written); stats:
+ * nrhs entries (seconds: the whole batch). */
+typedef struct gbds_bsolver_s *gbds_bsolver;
+int gbds_bsolver_create(gbds_bsolver *s, const int dims[4], int nrhs, const gbds_solver_params *p);
+int gbds_bsolver_destroy(gbds_bsolver s);
+int gbds_bsolver_set_gauge(gbds_bsolver s, const double *u_packed, void *stream);
+int gbds_bsolver_solve(gbds_bsolver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Reference entry points with precision suffixes                            */
 /* ------------------------------------------------------------------------ */

@@ -96,6 +96,10 @@ def core() -> ctypes.CDLL:
     L.gbds_solver_apply.argtypes = [vp, vp, vp, i, vp]
     L.gbds_solver_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
     L.gbds_solver_solve_normal.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
+    L.gbds_bsolver_create.argtypes = [ctypes.POINTER(vp), c_int_p, i, ctypes.POINTER(SolverParams)]
+    L.gbds_bsolver_destroy.argtypes = [vp]
+    L.gbds_bsolver_set_gauge.argtypes = [vp, vp, vp]
+    L.gbds_bsolver_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
     L.gbds_op_force.argtypes = [vp, vp, vp, vp, i, i, i, ctypes.c_double, i, vp, vp]
     L.gbds_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(BatchItem), i, i, i]
     L.gbds_batch_destroy.argtypes = [vp]

@@ -211,7 +211,26 @@ __device__ __forceinline__ void gen_hop_pair(const GenArgs &a, int h, int r, con
     reconstruct<MU, -ISIGN>(acc, w);
 }
 
-// One thread per (site, rhs); 4D.  EPI = 1 adds the xpay epilogue.
+// Per-rhs sums over a 128-thread block of (site, rhs) threads, rhs fastest:
+// partials[blockIdx.x * NRHS + r].  Lanes l and l + k NRHS of a warp hold
+// the same rhs.
+template <int NRHS>
+__device__ __forceinline__ void block_sum_rhs(double *partials, float v) {
+    static_assert(NRHS >= 2 && NRHS <= 32 && 32 % NRHS == 0, "NRHS must divide the warp");
+#pragma unroll
+    for (int o = 16; o >= NRHS; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ double ws[4][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane < NRHS) ws[w][lane] = (double)v;
+    __syncthreads();
+    if (threadIdx.x < NRHS)
+        partials[(size_t)blockIdx.x * NRHS + threadIdx.x] =
+            ws[0][threadIdx.x] + ws[1][threadIdx.x] + ws[2][threadIdx.x] + ws[3][threadIdx.x];
+}
+
+// One thread per (site, rhs); 4D.  EPI = 1 adds the xpay epilogue
+// (res = x + coef * D psi) with one |res|^2 partial per block; EPI = 2 the
+// same with one partial per block and rhs (NRHS 2..32, 128-thread blocks).
 template <int FMT, int RECON, int ISIGN, int NRHS, int EPI, int LFMT = 0>
 __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -246,8 +265,10 @@ __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
         }
         Sio<FMT>::store(a.res, a.cs, i, acc);
     }
-    if constexpr (EPI) {
+    if constexpr (EPI == 1) {
         if (a.partials) block_sum_to<float>(a.partials, nrm);
+    } else if constexpr (EPI == 2) {
+        if (a.partials) block_sum_rhs<NRHS>(a.partials, nrm);
     }
 }
 

@@ -40,16 +40,19 @@ __global__ void unpack_gen_kernel(const char *in, const int *__restrict__ table,
     }
 }
 
+// EPI: 0 none, 1 xpay (nrhs 1), 2 xpay with per-rhs partials (nrhs 2..32,
+// powers of two)
 template <int FMT, int RECON, int ISIGN, int EPI>
 void launch_gen_nrhs(const GenArgs &a, int nrhs, dim3 grid, cudaStream_t st) {
+    constexpr int E1 = EPI == 1 ? 1 : 0;  // nrhs 1 takes the single-sum epilogue
     switch (nrhs) {
-    case 1: dslash_gen_kernel<FMT, RECON, ISIGN, 1, EPI><<<grid, 128, 0, st>>>(a); break;
-    case 2: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 2, 0><<<grid, 128, 0, st>>>(a); break;
-    case 4: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 4, 0><<<grid, 128, 0, st>>>(a); break;
-    case 8: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 8, 0><<<grid, 128, 0, st>>>(a); break;
-    case 16: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 16, 0><<<grid, 128, 0, st>>>(a); break;
-    case 32: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 32, 0><<<grid, 128, 0, st>>>(a); break;
-    default: if constexpr (!EPI) dslash_gen_kernel<FMT, RECON, ISIGN, 0, 0><<<grid, 128, 0, st>>>(a); break;
+    case 1: if constexpr (EPI != 2) dslash_gen_kernel<FMT, RECON, ISIGN, 1, E1><<<grid, 128, 0, st>>>(a); break;
+    case 2: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 2, EPI><<<grid, 128, 0, st>>>(a); break;
+    case 4: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 4, EPI><<<grid, 128, 0, st>>>(a); break;
+    case 8: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 8, EPI><<<grid, 128, 0, st>>>(a); break;
+    case 16: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 16, EPI><<<grid, 128, 0, st>>>(a); break;
+    case 32: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 32, EPI><<<grid, 128, 0, st>>>(a); break;
+    default: if constexpr (EPI == 0) dslash_gen_kernel<FMT, RECON, ISIGN, 0, 0><<<grid, 128, 0, st>>>(a); break;
     }
 }
 
@@ -101,10 +104,12 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     const long long n = (long long)g.Vh * nrhs;
     const dim3 grid((unsigned)((n + 127) / 128));
     const bool epi = x != nullptr;
-    if (epi && nrhs != 1) return cudaErrorInvalidValue;
+    // the xpay epilogue takes nrhs 1 or a power of two up to 32
+    if (epi && (nrhs > 32 || (nrhs & (nrhs - 1)) != 0)) return cudaErrorInvalidValue;
 #define GBDS_GEN(R, S)                                                   \
     do {                                                                 \
-        if (epi) launch_gen_nrhs<FMT, R, S, 1>(a, nrhs, grid, st);       \
+        if (epi && nrhs == 1) launch_gen_nrhs<FMT, R, S, 1>(a, nrhs, grid, st);  \
+        else if (epi) launch_gen_nrhs<FMT, R, S, 2>(a, nrhs, grid, st);  \
         else launch_gen_nrhs<FMT, R, S, 0>(a, nrhs, grid, st);           \
     } while (0)
     if (recon == 18) { if (isign > 0) GBDS_GEN(18, 1); else GBDS_GEN(18, -1); }

@@ -21,9 +21,11 @@
 // convergence.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <vector>
 
 #include "dslash_gen.cuh"
 
@@ -714,5 +716,451 @@ static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, g
     out.converged = out.residual <= s->prm.tol ? 1 : 0;
     out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = out;
+    return GBDS_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Batched solve: nrhs independent systems M x_k = b_k on one gauge field.
+// The inner FP32 CGs of all right-hand sides advance in lockstep on the
+// multi-RHS operator (rhs fastest in memory: every link load serves all of
+// them), each with its own scalars and its own stopping point; a converged
+// right-hand side is masked out of the vector updates.  The FP64 defect
+// correction (residual, solution update, norms) is done per right-hand side
+// with the FP64 operator.
+// ---------------------------------------------------------------------------
+
+namespace gbds {
+namespace {
+
+struct BScalars {
+    double rr, pAp, alpha, beta;
+    int active;
+    int pad;
+};
+
+enum BFinish { kBAlpha = 0, kBBeta = 1, kBSetRR = 2 };
+
+// x += alpha_r p;  r -= alpha_r Ap;  per-rhs partial |r|^2  (active rhs only)
+template <int NRHS>
+__global__ void __launch_bounds__(128) bcg_update(float4 *x, float4 *r, const float4 *__restrict__ p,
+                                                 const float4 *__restrict__ Ap, const BScalars *sc, long long n, size_t cs,
+                                                 double *partials) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = (int)(t % NRHS);
+    float nrm = 0.f;
+    if (t < n && sc[q].active) {
+        const float a = (float)sc[q].alpha;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const size_t i = (size_t)k * cs + (size_t)t;
+            x[i] = axpy_v(a, p[i], x[i]);
+            const float4 rn = axpy_v(-a, Ap[i], r[i]);
+            r[i] = rn;
+            nrm += norm_v(rn);
+        }
+    }
+    block_sum_rhs<NRHS>(partials, nrm);
+}
+
+// p = r + beta_r p  (active rhs only)
+template <int NRHS>
+__global__ void __launch_bounds__(128) bcg_xpay(const float4 *__restrict__ r, float4 *p, const BScalars *sc, long long n,
+                                               size_t cs) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int q = (int)(t % NRHS);
+    if (!sc[q].active) return;
+    const float b = (float)sc[q].beta;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const size_t i = (size_t)k * cs + (size_t)t;
+        p[i] = axpy_v(b, p[i], r[i]);
+    }
+}
+
+// per-rhs partial |v|^2
+template <int NRHS>
+__global__ void __launch_bounds__(128) bnorm(const float4 *__restrict__ v, long long n, size_t cs, double *partials) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    float nrm = 0.f;
+    if (t < n) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) nrm += norm_v(v[(size_t)k * cs + (size_t)t]);
+    }
+    block_sum_rhs<NRHS>(partials, nrm);
+}
+
+// Per rhs (one block each): deterministic sum of its block partials, then the
+// scalar step.
+__global__ void __launch_bounds__(256) bfinish(const double *partials, int nblocks, int nrhs, BScalars *sc, int mode) {
+    __shared__ double buf[256];
+    const int q = blockIdx.x;
+    double t = 0;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) t += partials[(size_t)i * nrhs + q];
+    buf[threadIdx.x] = t;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) buf[threadIdx.x] += buf[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double sum = buf[0];
+    BScalars &c = sc[q];
+    switch (mode) {
+    case kBAlpha:
+        if (c.active) {
+            c.pAp = sum;
+            c.alpha = sum > 0 ? c.rr / sum : 0.0;
+        }
+        break;
+    case kBBeta:
+        if (c.active) {
+            c.beta = c.rr > 0 ? sum / c.rr : 0.0;
+            c.rr = sum;
+        }
+        break;
+    default: c.rr = sum; break;
+    }
+}
+
+// columns q of the multi-RHS inner fields: r = p = r64 / |r64|
+__global__ void __launch_bounds__(128) bdemote(const double2 *__restrict__ r64, double inv, float4 *r, float4 *p,
+                                              int Vh, int stride, int nrhs, int q, size_t cs) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const double2 a = r64[(size_t)(2 * k) * stride + h], b = r64[(size_t)(2 * k + 1) * stride + h];
+        const float4 f = make_float4((float)(a.x * inv), (float)(a.y * inv), (float)(b.x * inv), (float)(b.y * inv));
+        const size_t i = (size_t)k * cs + (size_t)h * nrhs + q;
+        r[i] = f;
+        p[i] = f;
+    }
+}
+
+// x64 += s * column q of e
+__global__ void __launch_bounds__(128) bpromote(const float4 *__restrict__ e, double s, double2 *x64, int Vh, int stride,
+                                               int nrhs, int q, size_t cs) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float4 v = e[(size_t)k * cs + (size_t)h * nrhs + q];
+        double2 &a = x64[(size_t)(2 * k) * stride + h];
+        double2 &b = x64[(size_t)(2 * k + 1) * stride + h];
+        a.x = fma(s, (double)v.x, a.x);
+        a.y = fma(s, (double)v.y, a.y);
+        b.x = fma(s, (double)v.z, b.x);
+        b.y = fma(s, (double)v.w, b.y);
+    }
+}
+
+}  // namespace
+}  // namespace gbds
+
+struct gbds_bsolver_s {
+    gbds_solver s1 = nullptr;  // FP64 gauge, FP64 operator temporaries, FP32 links, reductions
+    int nrhs = 0;
+    std::vector<void *> b64, c64, x64, r64;  // per rhs, FP64, checkerboard 0
+    void *e = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *Mp = nullptr, *t = nullptr;  // multi-RHS FP32
+    double *bpartials = nullptr;
+    BScalars *bsc = nullptr, *hbsc = nullptr;
+};
+
+namespace {
+
+long long bcount(gbds_bsolver b) { return (long long)b->s1->g.Vh * b->nrhs; }
+int bblocks(gbds_bsolver b) { return (int)((bcount(b) + 127) / 128); }
+size_t bcs(gbds_bsolver b) { return (size_t)b->s1->g.stride * b->nrhs; }
+
+#define GBDS_BN(NR, CALL) \
+    switch (NR) {         \
+    case 2: CALL(2); break; \
+    case 4: CALL(4); break; \
+    case 8: CALL(8); break; \
+    case 16: CALL(16); break; \
+    default: CALL(32); break; \
+    }
+
+cudaError_t bfinish_on(gbds_bsolver b, int mode, cudaStream_t st) {
+    bfinish<<<b->nrhs, 256, 0, st>>>(b->bpartials, bblocks(b), b->nrhs, b->bsc, mode);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// out = in - kappa^2 D_eo D_oe in for all rhs (partials: per-rhs |out|^2)
+cudaError_t apply_Mb(gbds_bsolver b, const void *in, void *out, int isign, double *partials, cudaStream_t st) {
+    gbds_solver s = b->s1;
+    const float k2 = (float)(s->prm.kappa * s->prm.kappa);
+    cudaError_t e =
+        launch_gen_f32(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, isign, 0, nullptr, 0.f, nullptr, st);
+    if (e != cudaSuccess) return e;
+    return launch_gen_f32(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, out, isign, 1, in, -k2, partials, st);
+}
+
+cudaError_t read_bscalars(gbds_bsolver b, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(b->hbsc, b->bsc, sizeof(BScalars) * b->nrhs, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
+// Lockstep CG on the active right-hand sides (x = e = 0, r = p = residual,
+// rr set); each stops at rr <= target[q] or when it stagnates.
+cudaError_t bcg(gbds_bsolver b, const std::vector<double> &target, int max_iter, std::vector<int> &iters,
+                cudaStream_t st) {
+    const long long n = bcount(b);
+    const int nb = bblocks(b);
+    const size_t cs = bcs(b);
+    const int nr = b->nrhs;
+    std::vector<double> best(nr, 1e300);
+    std::vector<int> best_k(nr, 0);
+    cudaError_t e = read_bscalars(b, st);
+    int k = 0;
+    while (e == cudaSuccess && k < max_iter) {
+        bool any = false;
+        for (int q = 0; q < nr; q++) any |= b->hbsc[q].active != 0;
+        if (!any) break;
+        e = apply_Mb(b, b->p, b->Mp, +1, b->bpartials, st);
+        if (e == cudaSuccess) e = bfinish_on(b, kBAlpha, st);
+        if (e == cudaSuccess) e = apply_Mb(b, b->Mp, b->Ap, -1, nullptr, st);
+        if (e == cudaSuccess) {
+#define GBDS_UPD(NR)                                                                                                 \
+    bcg_update<NR><<<nb, 128, 0, st>>>(static_cast<float4 *>(b->e), static_cast<float4 *>(b->r),                    \
+                                       static_cast<const float4 *>(b->p), static_cast<const float4 *>(b->Ap), b->bsc, n, \
+                                       cs, b->bpartials)
+            GBDS_BN(nr, GBDS_UPD)
+#undef GBDS_UPD
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = bfinish_on(b, kBBeta, st);
+        if (e == cudaSuccess) {
+#define GBDS_XP(NR) \
+    bcg_xpay<NR><<<nb, 128, 0, st>>>(static_cast<const float4 *>(b->r), static_cast<float4 *>(b->p), b->bsc, n, cs)
+            GBDS_BN(nr, GBDS_XP)
+#undef GBDS_XP
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e != cudaSuccess) break;
+        k++;
+        for (int q = 0; q < nr; q++)
+            if (b->hbsc[q].active) iters[q]++;
+        if (k % 4 == 0 || k == max_iter) {
+            e = read_bscalars(b, st);
+            if (e != cudaSuccess) break;
+            bool changed = false;
+            for (int q = 0; q < nr; q++) {
+                BScalars &c = b->hbsc[q];
+                if (!c.active) continue;
+                if (!(c.rr > target[q]) || stagnated(c.rr, k, best[q], best_k[q])) {
+                    c.active = 0;  // converged, stagnated or NaN
+                    changed = true;
+                }
+            }
+            if (changed) {
+                e = cudaMemcpyAsync(b->bsc, b->hbsc, sizeof(BScalars) * nr, cudaMemcpyHostToDevice, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            }
+        }
+    }
+    return e;
+}
+
+void brelease(gbds_bsolver b) {
+    for (auto *v : {&b->b64, &b->c64, &b->x64, &b->r64})
+        for (void *p : *v)
+            if (p) cudaFree(p);
+    void *bufs[] = {b->e, b->r, b->p, b->Ap, b->Mp, b->t, b->bpartials, b->bsc};
+    for (void *p : bufs)
+        if (p) cudaFree(p);
+    if (b->hbsc) cudaFreeHost(b->hbsc);
+    if (b->s1) gbds_solver_destroy(b->s1);
+}
+
+}  // namespace
+
+extern "C" int gbds_bsolver_create(gbds_bsolver *out, const int dims[4], int nrhs, const gbds_solver_params *p) {
+    if (!out || !p) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL argument");
+    *out = nullptr;
+    if (nrhs != 2 && nrhs != 4 && nrhs != 8 && nrhs != 16 && nrhs != 32)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "nrhs must be 2, 4, 8, 16 or 32");
+    if (p->inner_prec != 32) return set_error(GBDS_ERROR_UNSUPPORTED, "the batched solver runs an FP32 inner CG (inner_prec 32)");
+    gbds_bsolver b = new (std::nothrow) gbds_bsolver_s;
+    if (!b) return set_error(GBDS_ERROR_OUT_OF_MEMORY, "host allocation failed");
+    b->nrhs = nrhs;
+    int rc = gbds_solver_create(&b->s1, dims, p);
+    if (rc != GBDS_SUCCESS) {
+        delete b;
+        return rc;
+    }
+    const Geom &g = b->s1->g;
+    const size_t f64 = spinor_bytes(g, 64), f32m = spinor_bytes(g, 32) * nrhs;
+    cudaError_t e = cudaSuccess;
+    for (auto *v : {&b->b64, &b->c64, &b->x64, &b->r64}) {
+        v->assign(nrhs, nullptr);
+        for (int q = 0; q < nrhs && e == cudaSuccess; q++) e = cudaMalloc(&(*v)[q], f64);
+    }
+    void **bufs[] = {&b->e, &b->r, &b->p, &b->Ap, &b->Mp, &b->t};
+    for (void **x : bufs)
+        if (e == cudaSuccess) e = cudaMalloc(x, f32m);
+    if (e == cudaSuccess) e = cudaMalloc(&b->bpartials, sizeof(double) * (size_t)bblocks(b) * nrhs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->bsc, sizeof(BScalars) * nrhs);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->hbsc, sizeof(BScalars) * nrhs);
+    if (e != cudaSuccess) {
+        brelease(b);
+        delete b;
+        return cuda_error(e, "gbds_bsolver_create");
+    }
+    *out = b;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_bsolver_destroy(gbds_bsolver b) {
+    if (!b) return GBDS_SUCCESS;
+    cudaDeviceSynchronize();
+    brelease(b);
+    delete b;
+    return GBDS_SUCCESS;
+}
+
+extern "C" int gbds_bsolver_set_gauge(gbds_bsolver b, const double *u_packed, void *stream) {
+    if (!b) return set_error(GBDS_ERROR_NOT_INITIALIZED, "solver is NULL");
+    return gbds_solver_set_gauge(b->s1, u_packed, stream);
+}
+
+extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double *x_packed, gbds_solver_stats *stats,
+                                  void *stream) {
+    if (!b) return set_error(GBDS_ERROR_NOT_INITIALIZED, "solver is NULL");
+    gbds_solver s = b->s1;
+    if (!s->have_gauge) return set_error(GBDS_ERROR_NOT_INITIALIZED, "gbds_bsolver_set_gauge has not been called");
+    if (!b_packed || !x_packed) return set_error(GBDS_ERROR_INVALID_VALUE, "NULL field pointer");
+    if ((reinterpret_cast<uintptr_t>(b_packed) | reinterpret_cast<uintptr_t>(x_packed)) & 15u)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const auto t0 = std::chrono::steady_clock::now();
+    const Geom &g = s->g;
+    const int nr = b->nrhs;
+    const int nb1 = blocks(g);
+    const double tol2 = s->prm.tol * s->prm.tol;
+    const size_t vlen = (size_t)g.V * 24;  // doubles per packed right-hand side
+    std::vector<double> c2(nr, 0.0), b2(nr, 0.0), outer(nr, 0.0), bres(nr, 0.0);
+    std::vector<int> iters(nr, 0), cycles(nr, 0);
+    cudaError_t e = cudaSuccess;
+    // c_q = M^+ b_q, |c_q|^2, |b_q|^2, x_q = 0, r_q = c_q
+    for (int q = 0; q < nr && e == cudaSuccess; q++) {
+        e = launch_pack_spinor(g, 64, b_packed + q * vlen, nullptr, 0, 0, b->b64[q], st);
+        if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, b->b64[q], s->t64, b->c64[q], -1, nullptr, st);
+        if (e == cudaSuccess) e = norm_into<double>(s, b->c64[q], b->r64[q], nullptr, kOuterRR, st);
+        if (e == cudaSuccess) e = zero<double>(s, b->x64[q], st);
+        if (e == cudaSuccess) e = read_scalars(s, st);
+        if (e != cudaSuccess) break;
+        c2[q] = outer[q] = s->hsc->outer_rr;
+        e = norm_into<double>(s, b->b64[q], nullptr, nullptr, kNorm, st);
+        if (e == cudaSuccess) e = read_scalars(s, st);
+        b2[q] = s->hsc->norm;
+    }
+    int total = 0;
+    while (e == cudaSuccess && total < s->prm.max_iter) {
+        // right-hand sides still above the goal
+        std::vector<int> act;
+        for (int q = 0; q < nr; q++)
+            if (c2[q] > 0 && outer[q] > tol2 * c2[q]) act.push_back(q);
+        if (act.empty()) break;
+        const long long n = bcount(b);
+        const size_t cs = bcs(b);
+        for (void *v : {b->e, b->r, b->p}) {
+            if (e == cudaSuccess) e = cudaMemsetAsync(v, 0, spinor_bytes(g, 32) * nr, st);
+        }
+        std::vector<double> target(nr, 0.0);
+        for (int q = 0; q < nr; q++) {
+            b->hbsc[q] = BScalars{};
+            b->hbsc[q].active = 0;
+        }
+        for (int q : act) {
+            if (e != cudaSuccess) break;
+            bdemote<<<nb1, 128, 0, st>>>(static_cast<const double2 *>(b->r64[q]), 1.0 / std::sqrt(outer[q]),
+                                         static_cast<float4 *>(b->r), static_cast<float4 *>(b->p), g.Vh, g.stride, nr, q,
+                                         cs);
+            count_launch();
+            e = cudaGetLastError();
+            double delta = s->prm.inner_tol;
+            const double need = 0.5 * s->prm.tol * std::sqrt(c2[q] / outer[q]);
+            if (need > delta) delta = need;
+            target[q] = delta * delta;
+            b->hbsc[q].active = 1;
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->bsc, b->hbsc, sizeof(BScalars) * nr, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+#define GBDS_NRM(NR) bnorm<NR><<<bblocks(b), 128, 0, st>>>(static_cast<const float4 *>(b->r), n, cs, b->bpartials)
+            GBDS_BN(nr, GBDS_NRM)
+#undef GBDS_NRM
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = bfinish_on(b, kBSetRR, st);
+        std::vector<int> it(nr, 0);
+        if (e == cudaSuccess) e = bcg(b, target, s->prm.max_iter - total, it, st);
+        if (e != cudaSuccess) break;
+        int most = 0;
+        for (int q : act) {
+            iters[q] += it[q];
+            cycles[q]++;
+            most = std::max(most, it[q]);
+        }
+        total += most;
+        // x_q += |r_q| e_q; r_q = c_q - A x_q in FP64; |b_q - M x_q|
+        bool progress = false;
+        for (int q : act) {
+            if (e != cudaSuccess) break;
+            bpromote<<<nb1, 128, 0, st>>>(static_cast<const float4 *>(b->e), std::sqrt(outer[q]),
+                                          static_cast<double2 *>(b->x64[q]), g.Vh, g.stride, nr, q, cs);
+            count_launch();
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, b->x64[q], s->t64, s->Mp64, +1, nullptr, st);
+            if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->Mp64, s->t64, s->Ap64, -1, nullptr, st);
+            if (e == cudaSuccess) {
+                xmy_norm<<<nb1, kThreads, 0, st>>>(static_cast<const double2 *>(b->c64[q]),
+                                                   static_cast<const double2 *>(s->Ap64), static_cast<double2 *>(b->r64[q]),
+                                                   g.Vh, g.stride, s->partials);
+                count_launch();
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
+            if (e == cudaSuccess) {
+                xmy_norm<<<nb1, kThreads, 0, st>>>(static_cast<const double2 *>(b->b64[q]),
+                                                   static_cast<const double2 *>(s->Mp64), static_cast<double2 *>(s->p64),
+                                                   g.Vh, g.stride, s->partials);
+                count_launch();
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = finish_on(s, kNorm, st);
+            if (e == cudaSuccess) e = read_scalars(s, st);
+            if (e != cudaSuccess) break;
+            const double prev = outer[q];
+            outer[q] = s->hsc->outer_rr;
+            bres[q] = s->hsc->norm;
+            if (outer[q] < prev) progress = true;
+            else c2[q] = -c2[q];  // no progress (or NaN): stop this right-hand side, keep its last result
+        }
+        if (!progress) break;
+    }
+    for (int q = 0; q < nr && e == cudaSuccess; q++)
+        e = launch_unpack_spinor(g, 64, b->x64[q], nullptr, 0, 0, x_packed + q * vlen, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_bsolver_solve");
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) {
+        for (int q = 0; q < nr; q++) {
+            const double cc = std::fabs(c2[q]);
+            gbds_solver_stats &o = stats[q];
+            o.iterations = iters[q];
+            o.cycles = cycles[q];
+            o.residual = cc > 0 ? std::sqrt(outer[q] / cc) : 0.0;
+            o.true_residual = b2[q] > 0 && cycles[q] > 0 ? std::sqrt(bres[q] / b2[q]) : 0.0;
+            o.converged = o.residual <= s->prm.tol ? 1 : 0;
+            o.seconds = secs;
+        }
+    }
     return GBDS_SUCCESS;
 }

@@ -238,6 +238,52 @@ class WilsonSolver:
         return {k: getattr(st, k) for k, _ in st._fields_}
 
 
+class BatchedWilsonSolver:
+    """``nrhs`` (2, 4, 8, 16 or 32) independent solves M x_q = b_q on one gauge
+    field (gbds_bsolver_* in include/gbdslash.h): the FP32 inner CGs advance
+    together on the multi-RHS operator, the FP64 defect correction runs per
+    right-hand side.  b, x: FP64 CUDA tensors ``[nrhs][V][4][3][2]``."""
+
+    def __init__(self, dims, nrhs: int, kappa: float, tol: float = 1e-10, max_iter: int = 10000,
+                 inner_recon: int = 12, inner_tol: float = 1e-5):
+        self.dims = tuple(int(v) for v in dims)
+        self.volume = int(np.prod(self.dims))
+        self.nrhs = int(nrhs)
+        p = _lib.SolverParams(kappa, tol, max_iter, 32, inner_recon, inner_tol)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.core().gbds_bsolver_create(ctypes.byref(h), (ctypes.c_int * 4)(*self.dims), self.nrhs,
+                                                   ctypes.byref(p)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.core().gbds_bsolver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_gauge(self, u_packed, stream=None):
+        import torch
+        if u_packed.dtype != torch.float64 or u_packed.numel() < self.volume * 72:
+            raise ValueError("expected the FP64 packed gauge field")
+        _lib.check(_lib.core().gbds_bsolver_set_gauge(self._h, ctypes.c_void_p(_dptr(u_packed)), _stream(stream)))
+
+    def solve(self, b, x, stream=None) -> list:
+        import torch
+        n = self.nrhs * self.volume * 24
+        for t in (b, x):
+            if t.dtype != torch.float64 or t.numel() < n:
+                raise ValueError(f"expected float64 CUDA tensors with at least {n} elements")
+        st = (_lib.SolverStats * self.nrhs)()
+        _lib.check(_lib.core().gbds_bsolver_solve(self._h, ctypes.c_void_p(_dptr(b)), ctypes.c_void_p(_dptr(x)), st,
+                                                  _stream(stream)))
+        return [{k: getattr(s, k) for k, _ in s._fields_} for s in st]
+
+
 class DslashBatch:
     """Several lattices applied by one persistent launch (gbds_batch_* in
     include/gbdslash.h).  ``items``: list of dicts with keys op

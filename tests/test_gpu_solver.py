@@ -82,3 +82,55 @@ def test_mixed_and_fp64_solutions_agree():
         s.close()
     for x in xs[1:]:
         assert (xs[0] - x).norm() / xs[0].norm() < 1e-9
+
+
+@pytest.mark.parametrize("nrhs,inner_recon", [(4, 12), (8, 18)])
+def test_batched_solve_matches_single_solves(nrhs, inner_recon):
+    """The batched solver: every right-hand side reaches 1e-10, its solution
+    agrees with the single-rhs mixed solve of the same system, and the
+    oracle confirms |b - M x| / |b|.  One right-hand side is zero (its
+    solution stays zero) and two are multiples of each other (their
+    solutions are the same multiples)."""
+    import torch
+    from sse_wilson_dslash_gb300.device import BatchedWilsonSolver, WilsonSolver
+    dims = (8, 8, 8, 8)
+    V = O.volume(dims)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    u, _ = O.make_inputs(dims, 61, 62, kind="near_unit")
+    rng = np.random.default_rng(63)
+    bs = [O.gaussian_spinor(rng, V).ravel() for _ in range(nrhs)]
+    bs[1] = np.zeros_like(bs[1])
+    bs[3] = -2.5 * bs[2]
+    bsolver = BatchedWilsonSolver(dims, nrhs, KAPPA, tol=1e-10, inner_recon=inner_recon)
+    ug = torch.from_numpy(u.ravel()).cuda()
+    bsolver.set_gauge(ug)
+    bt = torch.from_numpy(np.stack(bs).ravel()).cuda()
+    xt = torch.zeros_like(bt)
+    stats = bsolver.solve(bt, xt)
+    x = xt.cpu().numpy().reshape(nrhs, V * 24)
+    single = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=32, inner_recon=inner_recon)
+    single.set_gauge(ug)
+    ev = O.target_sites(4, dims, lol, 1)
+    for q in range(nrhs):
+        if q == 1:
+            assert np.all(x[q] == 0.0) and stats[q]["iterations"] == 0
+            continue
+        assert stats[q]["converged"] == 1 and stats[q]["residual"] <= 1e-10, (q, stats[q])
+        Mx, _ = _even_M(dims, lol, u, x[q], KAPPA, 1)
+        num = np.linalg.norm((Mx - bs[q]).reshape(-1, 24)[ev])
+        assert num / np.linalg.norm(bs[q].reshape(-1, 24)[ev]) < 1e-9, q
+        xs = torch.zeros(V * 24, dtype=torch.float64, device="cuda")
+        single.solve(torch.from_numpy(bs[q].ravel()).cuda(), xs)
+        xs = xs.cpu().numpy().reshape(-1, 24)[ev]
+        assert np.linalg.norm(x[q].reshape(-1, 24)[ev] - xs) / np.linalg.norm(xs) < 1e-8, q
+    np.testing.assert_allclose(x[3].reshape(-1, 24)[ev], -2.5 * x[2].reshape(-1, 24)[ev], rtol=0, atol=1e-8 * np.abs(x[3]).max())
+    single.close()
+    bsolver.close()
+
+
+def test_batched_solver_rejects_bad_arguments():
+    from sse_wilson_dslash_gb300 import _lib
+    from sse_wilson_dslash_gb300.device import BatchedWilsonSolver
+    for kw in ({"nrhs": 3}, {"nrhs": 64}):
+        with pytest.raises(_lib.GbdsError):
+            BatchedWilsonSolver((4, 4, 4, 4), kw["nrhs"], KAPPA)
