@@ -192,6 +192,34 @@ def run_solver_bench(torch, log_fn):
     for k in ("mixed_fp32_fp64", "mixed_fp16_fp64", "mixed_bf16_fp64"):
         out[k]["speedup_vs_fp64"] = out["fp64_cg"]["wall_seconds"] / out[k]["wall_seconds"]
         out[k]["solution_rel_diff"] = float((sols["fp64_cg"] - sols[k]).norm() / sols["fp64_cg"].norm())
+    # batched: 16 right-hand sides (the first is the source above), FP32
+    # inner CGs in lockstep on the multi-RHS operator, FP64 defect correction
+    from sse_wilson_dslash_gb300.device import BatchedWilsonSolver
+    nrhs = 16
+    bb = torch.randn(nrhs, V * 24, dtype=torch.float64, device="cuda", generator=gen)
+    bb[0] = b
+    del sols
+    torch.cuda.empty_cache()
+    bs = BatchedWilsonSolver(dims, nrhs, 0.124, tol=1e-10, max_iter=20000, inner_recon=12)
+    bs.set_gauge(u)
+    xx = torch.zeros_like(bb)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sts = bs.solve(bb, xx)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    per_rhs = wall / nrhs
+    out["batched_fp32_fp64_nrhs16"] = {
+        "nrhs": nrhs, "wall_seconds": wall, "seconds_per_rhs": per_rhs,
+        "iterations_max": max(t["iterations"] for t in sts), "cycles_max": max(t["cycles"] for t in sts),
+        "converged": int(all(t["converged"] for t in sts)), "residual_max": max(t["residual"] for t in sts),
+        "true_residual_max": max(t["true_residual"] for t in sts),
+        "speedup_per_rhs_vs_fp64": out["fp64_cg"]["wall_seconds"] / per_rhs,
+        "speedup_per_rhs_vs_mixed_fp32": out["mixed_fp32_fp64"]["wall_seconds"] / per_rhs}
+    log_fn("batched_fp32_fp64_nrhs16", out["batched_fp32_fp64_nrhs16"])
+    bs.close()
+    del bs, bb, xx
+    torch.cuda.empty_cache()
     return out
 
 

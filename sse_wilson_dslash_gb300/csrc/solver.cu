@@ -8,8 +8,11 @@
 //   inner_prec 64: all-FP64 CG.
 //   inner_prec 32: FP32 CG (FP32 fields, FP32 arithmetic, per-block sums in
 //                  FP64) inside FP64 defect correction: the residual
-//                  r = c - A x, the solution update x += |r| e and all global
-//                  norms stay in FP64 on the GPU.
+//                  r = b - M x, the solution update and all global norms stay
+//                  in FP64 on the GPU; the inner right-hand side M^+ r is
+//                  formed in FP32 (two FP64 Dslash applications per cycle
+//                  instead of four).  The normal-equation solve keeps
+//                  r = c - A x in FP64.
 //   inner_prec 16 / 17: the same with the CG's direction p and the operator's
 //                  intermediates (M p, A p, D_oe p) stored as half with a
 //                  per-site norm (16) or bfloat16 (17), FP16 links, FP32
@@ -169,6 +172,50 @@ __global__ void __launch_bounds__(kThreads) promote_update(const float4 *__restr
     }
 }
 
+// r32 = inv * r64
+__global__ void __launch_bounds__(kThreads) demote_scaled(const double2 *__restrict__ r64, double inv, float4 *r32,
+                                                         int Vh, int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const double2 a = r64[(size_t)(2 * k) * stride + h], b = r64[(size_t)(2 * k + 1) * stride + h];
+        r32[(size_t)k * stride + h] =
+            make_float4((float)(a.x * inv), (float)(a.y * inv), (float)(b.x * inv), (float)(b.y * inv));
+    }
+}
+
+// r32 = a * v;  p32 = r32
+__global__ void __launch_bounds__(kThreads) scale_copy(const float4 *__restrict__ v, float a, float4 *r32, float4 *p32,
+                                                      int Vh, int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float4 x = v[(size_t)k * stride + h];
+        const float4 y = make_float4(a * x.x, a * x.y, a * x.z, a * x.w);
+        r32[(size_t)k * stride + h] = y;
+        p32[(size_t)k * stride + h] = y;
+    }
+}
+
+// x64 += s * e32
+__global__ void __launch_bounds__(kThreads) promote_scaled(const float4 *__restrict__ e32, double s, double2 *x64, int Vh,
+                                                          int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float4 e = e32[(size_t)k * stride + h];
+        double2 &a = x64[(size_t)(2 * k) * stride + h];
+        double2 &b = x64[(size_t)(2 * k + 1) * stride + h];
+        a.x = fma(s, (double)e.x, a.x);
+        a.y = fma(s, (double)e.y, a.y);
+        b.x = fma(s, (double)e.z, b.x);
+        b.y = fma(s, (double)e.w, b.y);
+    }
+}
+
 // --- 16-bit direction vectors (Sio formats), FP32 solution and residual ---
 
 // float4 component k of a spinor holds complexes 2k and 2k+1
@@ -232,6 +279,24 @@ __global__ void __launch_bounds__(kThreads) demote_residual_h(const double2 *__r
     for (int k = 0; k < 6; k++) {
         const double2 a = r64[(size_t)(2 * k) * stride + h], b = r64[(size_t)(2 * k + 1) * stride + h];
         const float4 f = make_float4((float)(a.x * s), (float)(a.y * s), (float)(b.x * s), (float)(b.y * s));
+        r32[(size_t)k * stride + h] = f;
+        ps[(2 * k) / 3][(2 * k) % 3] = {f.x, f.y};
+        ps[(2 * k + 1) / 3][(2 * k + 1) % 3] = {f.z, f.w};
+    }
+    Sio<FMT>::store(p, stride, h, ps);
+}
+
+// r32 = a * v;  p = r32 (16-bit)
+template <int FMT>
+__global__ void __launch_bounds__(kThreads) scale_copy_h(const float4 *__restrict__ v, float a, float4 *r32, char *p,
+                                                        int Vh, int stride) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Vh) return;
+    cx<float> ps[4][3];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float4 x = v[(size_t)k * stride + h];
+        const float4 f = make_float4(a * x.x, a * x.y, a * x.z, a * x.w);
         r32[(size_t)k * stride + h] = f;
         ps[(2 * k) / 3][(2 * k) % 3] = {f.x, f.y};
         ps[(2 * k + 1) / 3][(2 * k + 1) % 3] = {f.z, f.w};
@@ -494,7 +559,7 @@ extern "C" int gbds_solver_create(gbds_solver *out, const int dims[4], const gbd
     } else if (p->inner_prec == 16 || p->inner_prec == 17) {
         s->fmt16 = p->inner_prec == 16 ? kFmtF16N : kFmtBF16;
         const size_t f16 = (size_t)gen_spinor_bytes(s->fmt16) * g.stride;
-        void **d32[] = {&s->e32, &s->r32};
+        void **d32[] = {&s->e32, &s->r32, &s->Mp32, &s->t32};
         for (void **b : d32)
             if (e == cudaSuccess) e = cudaMalloc(b, f32);
         void **d16[] = {&s->p16, &s->Ap16, &s->Mp16, &s->t16};
@@ -575,6 +640,109 @@ extern "C" int gbds_solver_solve_normal(gbds_solver s, const double *c_packed, d
     return solve_impl(s, c_packed, x_packed, stats, stream, true);
 }
 
+// Mixed-precision solve of M x = b by defect correction on the true
+// residual: each cycle forms r = b - M x in FP64 (two FP64 Dslash
+// applications), then c = M^+ r in FP32 (the normal-equation right-hand side
+// for the inner CG and, through |c|, the stopping test |M^+ (b - M x)| <=
+// tol |M^+ b|: the cancellation is in the FP64 subtraction, so |c| carries
+// FP32 relative accuracy of its own size), then the inner CG on M^+ M and
+// x += |c| e in FP64.
+static int solve_mixed(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats,
+                       cudaStream_t st, std::chrono::steady_clock::time_point t0) {
+    const Geom &g = s->g;
+    const int nb = blocks(g);
+    const double tol2 = s->prm.tol * s->prm.tol;
+    const bool half = s->prm.inner_prec != 32;
+    gbds_solver_stats out = {};
+    cudaError_t e = launch_pack_spinor(g, 64, b_packed, nullptr, 0, 0, s->b64, st);
+    if (e == cudaSuccess) e = norm_into<double>(s, s->b64, s->r64, nullptr, kOuterRR, st);  // r = b
+    if (e == cudaSuccess) e = zero<double>(s, s->x64, st);
+    if (e == cudaSuccess) e = read_scalars(s, st);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");
+    const double b2 = s->hsc->outer_rr;
+    double r2 = b2;   // |b - M x|^2, FP64
+    double c2 = 0;    // |M^+ b|^2
+    double n2 = 0;    // |M^+ (b - M x)|^2
+    int total = 0;
+    bool stop = false;
+    while (b2 > 0) {
+        // c = M^+ (r / |r|) in FP32 and |c|^2
+        demote_scaled<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->r64), 1.0 / std::sqrt(r2),
+                                               static_cast<float4 *>(s->r32), g.Vh, g.stride);
+        count_launch();
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = apply_M<float>(s, s->gauge32, s->prm.inner_recon, s->r32, s->t32, s->Mp32, -1, s->partials, st);
+        if (e == cudaSuccess) e = finish_on(s, kNorm, st);
+        if (e == cudaSuccess) e = read_scalars(s, st);
+        if (e != cudaSuccess) break;
+        const double s2 = s->hsc->norm;
+        n2 = r2 * s2;
+        if (out.cycles == 0) c2 = n2;
+        if (stop || !(n2 > tol2 * c2) || total >= s->prm.max_iter || !(s2 > 0)) break;
+        // inner CG on A e = c / |c|, from e = 0
+        const float inv = (float)(1.0 / std::sqrt(s2));
+        if (!half)
+            scale_copy<<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->Mp32), inv, static_cast<float4 *>(s->r32),
+                                                static_cast<float4 *>(s->p32), g.Vh, g.stride);
+        else if (s->fmt16 == kFmtF16N)
+            scale_copy_h<kFmtF16N><<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->Mp32), inv,
+                                                            static_cast<float4 *>(s->r32), static_cast<char *>(s->p16),
+                                                            g.Vh, g.stride);
+        else
+            scale_copy_h<kFmtBF16><<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->Mp32), inv,
+                                                            static_cast<float4 *>(s->r32), static_cast<char *>(s->p16),
+                                                            g.Vh, g.stride);
+        count_launch();
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = zero<float>(s, s->e32, st);
+        if (e == cudaSuccess) e = norm_into<float>(s, s->r32, nullptr, nullptr, kSetRR, st);
+        if (e != cudaSuccess) break;
+        double delta = s->prm.inner_tol;
+        const double need = 0.5 * s->prm.tol * std::sqrt(c2 / n2);
+        if (need > delta) delta = need;
+        int it = 0;
+        if (!half)
+            e = cg<float>(s, s->gauge32, s->prm.inner_recon, s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32,
+                          delta * delta, s->prm.max_iter - total, &it, st);
+        else if (s->fmt16 == kFmtF16N)
+            e = cg_h<kFmtF16N>(s, delta * delta, s->prm.max_iter - total, &it, st);
+        else
+            e = cg_h<kFmtBF16>(s, delta * delta, s->prm.max_iter - total, &it, st);
+        total += it;
+        out.cycles++;
+        if (e != cudaSuccess) break;
+        // x += |c| e (the correction A^-1 M^+ r);  r = b - M x in FP64
+        promote_scaled<<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->e32), std::sqrt(n2),
+                                                static_cast<double2 *>(s->x64), g.Vh, g.stride);
+        count_launch();
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->x64, s->t64, s->Mp64, +1, nullptr, st);
+        if (e == cudaSuccess) {
+            xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->b64), static_cast<const double2 *>(s->Mp64),
+                                              static_cast<double2 *>(s->r64), g.Vh, g.stride, s->partials);
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
+        if (e == cudaSuccess) e = read_scalars(s, st);
+        if (e != cudaSuccess) break;
+        const double prev = r2;
+        r2 = s->hsc->outer_rr;
+        if (!(r2 < prev) || !(r2 > 0)) stop = true;  // no progress (or NaN, or exact): measure once more, then stop
+    }
+    if (e == cudaSuccess) e = launch_unpack_spinor(g, 64, s->x64, nullptr, 0, 0, x_packed, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "gbds_solver_solve");
+    out.iterations = total;
+    out.residual = c2 > 0 ? std::sqrt(n2 / c2) : 0.0;
+    out.true_residual = b2 > 0 ? std::sqrt(r2 / b2) : 0.0;
+    out.converged = out.residual <= s->prm.tol ? 1 : 0;
+    out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = out;
+    return GBDS_SUCCESS;
+}
+
 static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, gbds_solver_stats *stats, void *stream,
                       bool normal) {
     if (!s) return set_error(GBDS_ERROR_NOT_INITIALIZED, "solver is NULL");
@@ -584,6 +752,7 @@ static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, g
         return set_error(GBDS_ERROR_INVALID_VALUE, "fields must be 16-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const auto t0 = std::chrono::steady_clock::now();
+    if (!normal && s->prm.inner_prec != 64) return solve_mixed(s, b_packed, x_packed, stats, st, t0);
     gbds_solver_stats out = {};
     const Geom &g = s->g;
     const double tol2 = s->prm.tol * s->prm.tol;
@@ -823,6 +992,24 @@ __global__ void __launch_bounds__(256) bfinish(const double *partials, int nbloc
     }
 }
 
+// r = p = scale_q * v (scale in sc[q].beta; zero for inactive rhs)
+template <int NRHS>
+__global__ void __launch_bounds__(128) bscale_copy(const float4 *__restrict__ v, const BScalars *sc, float4 *r, float4 *p,
+                                                  long long n, size_t cs) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int q = (int)(t % NRHS);
+    const float a = sc[q].active ? (float)sc[q].beta : 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const size_t i = (size_t)k * cs + (size_t)t;
+        const float4 x = v[i];
+        const float4 y = make_float4(a * x.x, a * x.y, a * x.z, a * x.w);
+        r[i] = y;
+        p[i] = y;
+    }
+}
+
 // columns q of the multi-RHS inner fields: r = p = r64 / |r64|
 __global__ void __launch_bounds__(128) bdemote(const double2 *__restrict__ r64, double inv, float4 *r, float4 *p,
                                               int Vh, int stride, int nrhs, int q, size_t cs) {
@@ -861,7 +1048,7 @@ __global__ void __launch_bounds__(128) bpromote(const float4 *__restrict__ e, do
 struct gbds_bsolver_s {
     gbds_solver s1 = nullptr;  // FP64 gauge, FP64 operator temporaries, FP32 links, reductions
     int nrhs = 0;
-    std::vector<void *> b64, c64, x64, r64;  // per rhs, FP64, checkerboard 0
+    std::vector<void *> b64, x64, r64;  // per rhs, FP64, checkerboard 0
     void *e = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *Mp = nullptr, *t = nullptr;  // multi-RHS FP32
     double *bpartials = nullptr;
     BScalars *bsc = nullptr, *hbsc = nullptr;
@@ -968,7 +1155,7 @@ cudaError_t bcg(gbds_bsolver b, const std::vector<double> &target, int max_iter,
 }
 
 void brelease(gbds_bsolver b) {
-    for (auto *v : {&b->b64, &b->c64, &b->x64, &b->r64})
+    for (auto *v : {&b->b64, &b->x64, &b->r64})
         for (void *p : *v)
             if (p) cudaFree(p);
     void *bufs[] = {b->e, b->r, b->p, b->Ap, b->Mp, b->t, b->bpartials, b->bsc};
@@ -997,7 +1184,7 @@ extern "C" int gbds_bsolver_create(gbds_bsolver *out, const int dims[4], int nrh
     const Geom &g = b->s1->g;
     const size_t f64 = spinor_bytes(g, 64), f32m = spinor_bytes(g, 32) * nrhs;
     cudaError_t e = cudaSuccess;
-    for (auto *v : {&b->b64, &b->c64, &b->x64, &b->r64}) {
+    for (auto *v : {&b->b64, &b->x64, &b->r64}) {
         v->assign(nrhs, nullptr);
         for (int q = 0; q < nrhs && e == cudaSuccess; q++) e = cudaMalloc(&(*v)[q], f64);
     }
@@ -1042,55 +1229,79 @@ extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double
     const Geom &g = s->g;
     const int nr = b->nrhs;
     const int nb1 = blocks(g);
+    const long long n = bcount(b);
+    const size_t cs = bcs(b);
     const double tol2 = s->prm.tol * s->prm.tol;
     const size_t vlen = (size_t)g.V * 24;  // doubles per packed right-hand side
-    std::vector<double> c2(nr, 0.0), b2(nr, 0.0), outer(nr, 0.0), bres(nr, 0.0);
+    // per rhs: |b|^2, |b - M x|^2 (FP64), |M^+ b|^2, |M^+ (b - M x)|^2
+    std::vector<double> b2(nr, 0.0), r2(nr, 0.0), c2(nr, 0.0), n2(nr, 0.0);
     std::vector<int> iters(nr, 0), cycles(nr, 0);
+    std::vector<char> live(nr, 0);  // still being solved
+    std::vector<char> last(nr, 0);  // no progress in the last cycle: measure once more, then stop
     cudaError_t e = cudaSuccess;
-    // c_q = M^+ b_q, |c_q|^2, |b_q|^2, x_q = 0, r_q = c_q
     for (int q = 0; q < nr && e == cudaSuccess; q++) {
         e = launch_pack_spinor(g, 64, b_packed + q * vlen, nullptr, 0, 0, b->b64[q], st);
-        if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, b->b64[q], s->t64, b->c64[q], -1, nullptr, st);
-        if (e == cudaSuccess) e = norm_into<double>(s, b->c64[q], b->r64[q], nullptr, kOuterRR, st);
+        if (e == cudaSuccess) e = norm_into<double>(s, b->b64[q], b->r64[q], nullptr, kOuterRR, st);  // r = b
         if (e == cudaSuccess) e = zero<double>(s, b->x64[q], st);
         if (e == cudaSuccess) e = read_scalars(s, st);
         if (e != cudaSuccess) break;
-        c2[q] = outer[q] = s->hsc->outer_rr;
-        e = norm_into<double>(s, b->b64[q], nullptr, nullptr, kNorm, st);
-        if (e == cudaSuccess) e = read_scalars(s, st);
-        b2[q] = s->hsc->norm;
+        b2[q] = r2[q] = s->hsc->outer_rr;
+        live[q] = b2[q] > 0;
     }
     int total = 0;
-    while (e == cudaSuccess && total < s->prm.max_iter) {
-        // right-hand sides still above the goal
-        std::vector<int> act;
-        for (int q = 0; q < nr; q++)
-            if (c2[q] > 0 && outer[q] > tol2 * c2[q]) act.push_back(q);
-        if (act.empty()) break;
-        const long long n = bcount(b);
-        const size_t cs = bcs(b);
-        for (void *v : {b->e, b->r, b->p}) {
-            if (e == cudaSuccess) e = cudaMemsetAsync(v, 0, spinor_bytes(g, 32) * nr, st);
-        }
-        std::vector<double> target(nr, 0.0);
-        for (int q = 0; q < nr; q++) {
-            b->hbsc[q] = BScalars{};
-            b->hbsc[q].active = 0;
-        }
-        for (int q : act) {
-            if (e != cudaSuccess) break;
-            bdemote<<<nb1, 128, 0, st>>>(static_cast<const double2 *>(b->r64[q]), 1.0 / std::sqrt(outer[q]),
+    bool first = true;
+    while (e == cudaSuccess) {
+        // c_q = M^+ (r_q / |r_q|) in FP32 for all right-hand sides at once, and |c_q|^2
+        e = cudaMemsetAsync(b->r, 0, spinor_bytes(g, 32) * nr, st);
+        for (int q = 0; q < nr && e == cudaSuccess; q++) {
+            if (!live[q]) continue;
+            bdemote<<<nb1, 128, 0, st>>>(static_cast<const double2 *>(b->r64[q]), 1.0 / std::sqrt(r2[q]),
                                          static_cast<float4 *>(b->r), static_cast<float4 *>(b->p), g.Vh, g.stride, nr, q,
                                          cs);
             count_launch();
             e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = apply_Mb(b, b->r, b->Mp, -1, b->bpartials, st);
+        for (int q = 0; q < nr; q++) b->hbsc[q] = BScalars{};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->bsc, b->hbsc, sizeof(BScalars) * nr, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = bfinish_on(b, kBSetRR, st);
+        if (e == cudaSuccess) e = read_bscalars(b, st);
+        if (e != cudaSuccess) break;
+        std::vector<double> target(nr, 0.0);
+        bool any = false;
+        for (int q = 0; q < nr; q++) {
+            const double s2 = b->hbsc[q].rr;
+            BScalars &c = b->hbsc[q];
+            c = BScalars{};
+            if (!live[q]) continue;
+            n2[q] = r2[q] * s2;
+            if (first) c2[q] = n2[q];
+            if (last[q] || !(n2[q] > tol2 * c2[q]) || total >= s->prm.max_iter || !(s2 > 0)) {
+                live[q] = 0;  // converged, stalled, or nothing left to solve
+                continue;
+            }
             double delta = s->prm.inner_tol;
-            const double need = 0.5 * s->prm.tol * std::sqrt(c2[q] / outer[q]);
+            const double need = 0.5 * s->prm.tol * std::sqrt(c2[q] / n2[q]);
             if (need > delta) delta = need;
             target[q] = delta * delta;
-            b->hbsc[q].active = 1;
+            c.active = 1;
+            c.beta = 1.0 / std::sqrt(s2);  // scale of the inner right-hand side
+            any = true;
         }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(b->bsc, b->hbsc, sizeof(BScalars) * nr, cudaMemcpyHostToDevice, st);
+        first = false;
+        if (!any) break;
+        // inner CG on A e_q = c_q / |c_q| from e = 0
+        e = cudaMemcpyAsync(b->bsc, b->hbsc, sizeof(BScalars) * nr, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+#define GBDS_SC(NR)                                                                                                  \
+    bscale_copy<NR><<<bblocks(b), 128, 0, st>>>(static_cast<const float4 *>(b->Mp), b->bsc, static_cast<float4 *>(b->r), \
+                                                static_cast<float4 *>(b->p), n, cs)
+            GBDS_BN(nr, GBDS_SC)
+#undef GBDS_SC
+            count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->e, 0, spinor_bytes(g, 32) * nr, st);
         if (e == cudaSuccess) {
 #define GBDS_NRM(NR) bnorm<NR><<<bblocks(b), 128, 0, st>>>(static_cast<const float4 *>(b->r), n, cs, b->bpartials)
             GBDS_BN(nr, GBDS_NRM)
@@ -1103,47 +1314,35 @@ extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double
         if (e == cudaSuccess) e = bcg(b, target, s->prm.max_iter - total, it, st);
         if (e != cudaSuccess) break;
         int most = 0;
-        for (int q : act) {
+        for (int q = 0; q < nr; q++) {
+            if (target[q] == 0.0) continue;
             iters[q] += it[q];
             cycles[q]++;
             most = std::max(most, it[q]);
         }
         total += most;
-        // x_q += |r_q| e_q; r_q = c_q - A x_q in FP64; |b_q - M x_q|
-        bool progress = false;
-        for (int q : act) {
-            if (e != cudaSuccess) break;
-            bpromote<<<nb1, 128, 0, st>>>(static_cast<const float4 *>(b->e), std::sqrt(outer[q]),
+        // x_q += |c_q| e_q;  r_q = b_q - M x_q in FP64
+        for (int q = 0; q < nr && e == cudaSuccess; q++) {
+            if (target[q] == 0.0) continue;
+            bpromote<<<nb1, 128, 0, st>>>(static_cast<const float4 *>(b->e), std::sqrt(n2[q]),
                                           static_cast<double2 *>(b->x64[q]), g.Vh, g.stride, nr, q, cs);
             count_launch();
             e = cudaGetLastError();
             if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, b->x64[q], s->t64, s->Mp64, +1, nullptr, st);
-            if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->Mp64, s->t64, s->Ap64, -1, nullptr, st);
             if (e == cudaSuccess) {
-                xmy_norm<<<nb1, kThreads, 0, st>>>(static_cast<const double2 *>(b->c64[q]),
-                                                   static_cast<const double2 *>(s->Ap64), static_cast<double2 *>(b->r64[q]),
+                xmy_norm<<<nb1, kThreads, 0, st>>>(static_cast<const double2 *>(b->b64[q]),
+                                                   static_cast<const double2 *>(s->Mp64), static_cast<double2 *>(b->r64[q]),
                                                    g.Vh, g.stride, s->partials);
                 count_launch();
                 e = cudaGetLastError();
             }
             if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
-            if (e == cudaSuccess) {
-                xmy_norm<<<nb1, kThreads, 0, st>>>(static_cast<const double2 *>(b->b64[q]),
-                                                   static_cast<const double2 *>(s->Mp64), static_cast<double2 *>(s->p64),
-                                                   g.Vh, g.stride, s->partials);
-                count_launch();
-                e = cudaGetLastError();
-            }
-            if (e == cudaSuccess) e = finish_on(s, kNorm, st);
             if (e == cudaSuccess) e = read_scalars(s, st);
             if (e != cudaSuccess) break;
-            const double prev = outer[q];
-            outer[q] = s->hsc->outer_rr;
-            bres[q] = s->hsc->norm;
-            if (outer[q] < prev) progress = true;
-            else c2[q] = -c2[q];  // no progress (or NaN): stop this right-hand side, keep its last result
+            const double prev = r2[q];
+            r2[q] = s->hsc->outer_rr;
+            if (!(r2[q] < prev) || !(r2[q] > 0)) last[q] = 1;  // no progress (or NaN, or exact)
         }
-        if (!progress) break;
     }
     for (int q = 0; q < nr && e == cudaSuccess; q++)
         e = launch_unpack_spinor(g, 64, b->x64[q], nullptr, 0, 0, x_packed + q * vlen, st);
@@ -1152,12 +1351,11 @@ extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) {
         for (int q = 0; q < nr; q++) {
-            const double cc = std::fabs(c2[q]);
             gbds_solver_stats &o = stats[q];
             o.iterations = iters[q];
             o.cycles = cycles[q];
-            o.residual = cc > 0 ? std::sqrt(outer[q] / cc) : 0.0;
-            o.true_residual = b2[q] > 0 && cycles[q] > 0 ? std::sqrt(bres[q] / b2[q]) : 0.0;
+            o.residual = c2[q] > 0 ? std::sqrt(n2[q] / c2[q]) : 0.0;
+            o.true_residual = b2[q] > 0 ? std::sqrt(r2[q] / b2[q]) : 0.0;
             o.converged = o.residual <= s->prm.tol ? 1 : 0;
             o.seconds = secs;
         }
