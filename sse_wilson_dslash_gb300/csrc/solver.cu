@@ -909,11 +909,11 @@ struct BScalars {
 
 enum BFinish { kBAlpha = 0, kBBeta = 1, kBSetRR = 2 };
 
-// x += alpha_r p;  r -= alpha_r Ap;  per-rhs partial |r|^2  (active rhs only)
+// r -= alpha_r Ap;  per-rhs partial |r|^2  (active rhs only; the matching
+// x += alpha_r p happens in bcg_xpay, which reads p anyway)
 template <int NRHS>
-__global__ void __launch_bounds__(128) bcg_update(float4 *x, float4 *r, const float4 *__restrict__ p,
-                                                 const float4 *__restrict__ Ap, const BScalars *sc, long long n, size_t cs,
-                                                 double *partials) {
+__global__ void __launch_bounds__(128) bcg_update(float4 *r, const float4 *__restrict__ Ap, const BScalars *sc, long long n,
+                                                 size_t cs, double *partials) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = (int)(t % NRHS);
     float nrm = 0.f;
@@ -922,7 +922,6 @@ __global__ void __launch_bounds__(128) bcg_update(float4 *x, float4 *r, const fl
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             const size_t i = (size_t)k * cs + (size_t)t;
-            x[i] = axpy_v(a, p[i], x[i]);
             const float4 rn = axpy_v(-a, Ap[i], r[i]);
             r[i] = rn;
             nrm += norm_v(rn);
@@ -931,19 +930,21 @@ __global__ void __launch_bounds__(128) bcg_update(float4 *x, float4 *r, const fl
     block_sum_rhs<NRHS>(partials, nrm);
 }
 
-// p = r + beta_r p  (active rhs only)
+// x += alpha_r p;  p = r + beta_r p  (active rhs only)
 template <int NRHS>
-__global__ void __launch_bounds__(128) bcg_xpay(const float4 *__restrict__ r, float4 *p, const BScalars *sc, long long n,
-                                               size_t cs) {
+__global__ void __launch_bounds__(128) bcg_xpay(float4 *x, const float4 *__restrict__ r, float4 *p, const BScalars *sc,
+                                               long long n, size_t cs) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int q = (int)(t % NRHS);
     if (!sc[q].active) return;
-    const float b = (float)sc[q].beta;
+    const float a = (float)sc[q].alpha, b = (float)sc[q].beta;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
         const size_t i = (size_t)k * cs + (size_t)t;
-        p[i] = axpy_v(b, p[i], r[i]);
+        const float4 pv = p[i];
+        x[i] = axpy_v(a, pv, x[i]);
+        p[i] = axpy_v(b, pv, r[i]);
     }
 }
 
@@ -959,21 +960,33 @@ __global__ void __launch_bounds__(128) bnorm(const float4 *__restrict__ v, long 
     block_sum_rhs<NRHS>(partials, nrm);
 }
 
-// Per rhs (one block each): deterministic sum of its block partials, then the
-// scalar step.
-__global__ void __launch_bounds__(256) bfinish(const double *partials, int nblocks, int nrhs, BScalars *sc, int mode) {
+// Per-rhs sums of the (block, rhs) partials in two fixed-order stages.
+// Stage 1: block j of the grid sums rows [j*rows, (j+1)*rows) for every rhs
+// (thread t takes rhs t % nrhs: coalesced reads) into partials2[j][rhs].
+constexpr int kBRows = 1024;  // partial rows per stage-1 block
+__global__ void __launch_bounds__(256) bfinish1(const double *partials, int nrows, int nrhs, double *partials2) {
     __shared__ double buf[256];
-    const int q = blockIdx.x;
+    const int q = threadIdx.x % nrhs, lanes = 256 / nrhs;  // nrhs divides 256
+    const int row0 = blockIdx.x * kBRows;
+    const int row1 = min(row0 + kBRows, nrows);
     double t = 0;
-    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) t += partials[(size_t)i * nrhs + q];
+    for (int i = row0 + threadIdx.x / nrhs; i < row1; i += lanes) t += partials[(size_t)i * nrhs + q];
     buf[threadIdx.x] = t;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) buf[threadIdx.x] += buf[threadIdx.x + s];
-        __syncthreads();
+    if (threadIdx.x < nrhs) {
+        double s = 0;
+        for (int j = 0; j < lanes; j++) s += buf[j * nrhs + threadIdx.x];
+        partials2[(size_t)blockIdx.x * nrhs + threadIdx.x] = s;
     }
-    if (threadIdx.x != 0) return;
-    const double sum = buf[0];
+}
+
+// Stage 2: per rhs (thread), the sum over the stage-1 blocks, then the
+// scalar step.
+__global__ void __launch_bounds__(32) bfinish2(const double *partials2, int nblocks2, int nrhs, BScalars *sc, int mode) {
+    const int q = threadIdx.x;
+    if (q >= nrhs) return;
+    double sum = 0;
+    for (int j = 0; j < nblocks2; j++) sum += partials2[(size_t)j * nrhs + q];
     BScalars &c = sc[q];
     switch (mode) {
     case kBAlpha:
@@ -1050,7 +1063,7 @@ struct gbds_bsolver_s {
     int nrhs = 0;
     std::vector<void *> b64, x64, r64;  // per rhs, FP64, checkerboard 0
     void *e = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *Mp = nullptr, *t = nullptr;  // multi-RHS FP32
-    double *bpartials = nullptr;
+    double *bpartials = nullptr, *bpartials2 = nullptr;
     BScalars *bsc = nullptr, *hbsc = nullptr;
 };
 
@@ -1069,9 +1082,12 @@ size_t bcs(gbds_bsolver b) { return (size_t)b->s1->g.stride * b->nrhs; }
     default: CALL(32); break; \
     }
 
+int bblocks2(gbds_bsolver b) { return (bblocks(b) + kBRows - 1) / kBRows; }
+
 cudaError_t bfinish_on(gbds_bsolver b, int mode, cudaStream_t st) {
-    bfinish<<<b->nrhs, 256, 0, st>>>(b->bpartials, bblocks(b), b->nrhs, b->bsc, mode);
-    count_launch();
+    bfinish1<<<bblocks2(b), 256, 0, st>>>(b->bpartials, bblocks(b), b->nrhs, b->bpartials2);
+    bfinish2<<<1, 32, 0, st>>>(b->bpartials2, bblocks2(b), b->nrhs, b->bsc, mode);
+    count_launch(2);
     return cudaGetLastError();
 }
 
@@ -1111,9 +1127,8 @@ cudaError_t bcg(gbds_bsolver b, const std::vector<double> &target, int max_iter,
         if (e == cudaSuccess) e = bfinish_on(b, kBAlpha, st);
         if (e == cudaSuccess) e = apply_Mb(b, b->Mp, b->Ap, -1, nullptr, st);
         if (e == cudaSuccess) {
-#define GBDS_UPD(NR)                                                                                                 \
-    bcg_update<NR><<<nb, 128, 0, st>>>(static_cast<float4 *>(b->e), static_cast<float4 *>(b->r),                    \
-                                       static_cast<const float4 *>(b->p), static_cast<const float4 *>(b->Ap), b->bsc, n, \
+#define GBDS_UPD(NR)                                                                                      \
+    bcg_update<NR><<<nb, 128, 0, st>>>(static_cast<float4 *>(b->r), static_cast<const float4 *>(b->Ap), b->bsc, n, \
                                        cs, b->bpartials)
             GBDS_BN(nr, GBDS_UPD)
 #undef GBDS_UPD
@@ -1122,8 +1137,9 @@ cudaError_t bcg(gbds_bsolver b, const std::vector<double> &target, int max_iter,
         }
         if (e == cudaSuccess) e = bfinish_on(b, kBBeta, st);
         if (e == cudaSuccess) {
-#define GBDS_XP(NR) \
-    bcg_xpay<NR><<<nb, 128, 0, st>>>(static_cast<const float4 *>(b->r), static_cast<float4 *>(b->p), b->bsc, n, cs)
+#define GBDS_XP(NR)                                                                                         \
+    bcg_xpay<NR><<<nb, 128, 0, st>>>(static_cast<float4 *>(b->e), static_cast<const float4 *>(b->r),               \
+                                     static_cast<float4 *>(b->p), b->bsc, n, cs)
             GBDS_BN(nr, GBDS_XP)
 #undef GBDS_XP
             count_launch();
@@ -1158,7 +1174,7 @@ void brelease(gbds_bsolver b) {
     for (auto *v : {&b->b64, &b->x64, &b->r64})
         for (void *p : *v)
             if (p) cudaFree(p);
-    void *bufs[] = {b->e, b->r, b->p, b->Ap, b->Mp, b->t, b->bpartials, b->bsc};
+    void *bufs[] = {b->e, b->r, b->p, b->Ap, b->Mp, b->t, b->bpartials, b->bpartials2, b->bsc};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (b->hbsc) cudaFreeHost(b->hbsc);
@@ -1192,6 +1208,7 @@ extern "C" int gbds_bsolver_create(gbds_bsolver *out, const int dims[4], int nrh
     for (void **x : bufs)
         if (e == cudaSuccess) e = cudaMalloc(x, f32m);
     if (e == cudaSuccess) e = cudaMalloc(&b->bpartials, sizeof(double) * (size_t)bblocks(b) * nrhs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->bpartials2, sizeof(double) * (size_t)bblocks2(b) * nrhs);
     if (e == cudaSuccess) e = cudaMalloc(&b->bsc, sizeof(BScalars) * nrhs);
     if (e == cudaSuccess) e = cudaMallocHost(&b->hbsc, sizeof(BScalars) * nrhs);
     if (e != cudaSuccess) {
