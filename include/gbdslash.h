@@ -146,9 +146,11 @@ int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
                    int isign, int cb, void *stream);
 
 /* Launch tuning of gbds_op_dslash: threads per block (0 = default 128; a
- * multiple of 32 up to 256) and a kernel variant (0 = registers uncapped;
- * 1.. = variants that cap registers for more resident warps, which launch
- * 128-thread blocks).  gbds_op_num_variants gives the count.  Used by the
+ * multiple of 32 up to 256) and a kernel variant.  Single rhs: 0 = registers
+ * uncapped; 1.. = variants that cap registers for more resident warps, which
+ * launch 128-thread blocks.  Several rhs or 16-bit storage: 0 = the plain
+ * multi-RHS kernel, 1 = the packed FP32x2 form (8, 16, 32 rhs; the block
+ * size is fixed at 128).  gbds_op_num_variants gives the count.  Used by the
  * autotuner. */
 int gbds_op_set_tuning(gbds_op op, int threads, int variant);
 int gbds_op_get_tuning(gbds_op op, int *threads, int *variant);
@@ -157,10 +159,12 @@ int gbds_op_num_variants(gbds_op op);
 /* Time every (block, variant) candidate of gbds_op_dslash on the caller's
  * fields (res is overwritten), keep the fastest for this operator and cache
  * it process-wide for its (dims, nd, prec, recon, nrhs, format); a later call
- * for the same shape takes the cached choice without timing.  For 16-bit
- * formats with 16 or 32 right-hand sides the candidates are the CUDA-core and
- * the tensor-core kernels (gbds_op_set_tensor_cores); other operators with
- * several right-hand sides have nothing to tune.  Synchronises `stream`. */
+ * for the same shape takes the cached choice without timing.  Operators with
+ * several right-hand sides (or 16-bit storage) have two variants: 0 the plain
+ * multi-RHS kernel, 1 the colour multiply in packed FP32x2 arithmetic on
+ * links staged per CTA (8, 16 or 32 rhs); for 16-bit formats with 16 or 32
+ * rhs the tensor-core kernel (gbds_op_set_tensor_cores) is a third
+ * candidate.  Synchronises `stream`. */
 int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream);
 
 /* Number of kernels this library has launched in this process (all kinds). */

@@ -116,9 +116,14 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     // for 6 blocks of 128 threads per SM, FP32 recon 12 with 64-thread blocks,
     // FP64 (FP64-issue bound) is insensitive.
     o->block = (prec == 32 && recon == 12) ? 64 : 128;
-    o->variant = (prec == 32 && recon == 18) ? 1 : 0;
     o->nrhs = nrhs;
     o->format = format;
+    // Single rhs: the register-cap variant (see above).  Several rhs or
+    // 16-bit storage: variant 0 = the plain multi-RHS kernel, 1 = its packed
+    // FP32x2 form (nrhs 8, 16, 32), measured faster from 16 rhs on at
+    // 24^3x48 (autotune chooses per shape).
+    const bool gen = nrhs > 1 || format != GBDS_SPINOR_NATIVE;
+    o->variant = gen ? (nrhs >= 16 ? 1 : 0) : ((prec == 32 && recon == 18) ? 1 : 0);
     o->tensor_cores = 0;
     o->d_err = nullptr;
     o->d_site_table = nullptr;
@@ -228,14 +233,17 @@ extern "C" int gbds_op_set_tuning(gbds_op op, int threads, int variant) {
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
     if (threads != 0 && (threads < 32 || threads > 256 || threads % 32 != 0))
         return set_error(GBDS_ERROR_INVALID_VALUE, "block must be 0 or a multiple of 32 in [32, 256]");
-    if (variant < 0 || variant >= dslash_variants(op->prec))
+    if (variant < 0 || variant >= gbds_op_num_variants(op))
         return set_error(GBDS_ERROR_INVALID_VALUE, "variant out of range");
     op->block = threads;
     op->variant = variant;
     return GBDS_SUCCESS;
 }
 
-extern "C" int gbds_op_num_variants(gbds_op op) { return op ? dslash_variants(op->prec) : 0; }
+extern "C" int gbds_op_num_variants(gbds_op op) {
+    if (!op) return 0;
+    return (op->nrhs > 1 || op->format != GBDS_SPINOR_NATIVE) ? 2 : dslash_variants(op->prec);
+}
 
 namespace {
 std::mutex g_tune_mutex;
@@ -249,9 +257,11 @@ static bool tc_eligible(gbds_op op) {
 
 extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream) {
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
-    // several right-hand sides: the kernels take no block / variant choice;
-    // 16-bit storage with 16 or 32 of them chooses CUDA cores or tensor cores
-    if (generic(op) && !tc_eligible(op)) return GBDS_SUCCESS;
+    // several right-hand sides: the candidates are the plain kernel, its
+    // packed FP32x2 form (8, 16, 32 rhs) and, for 16-bit storage with 16 or
+    // 32 rhs, the tensor-core kernel
+    const bool v2ok = op->nrhs == 8 || op->nrhs == 16 || op->nrhs == 32;
+    if (generic(op) && !tc_eligible(op) && !v2ok) return GBDS_SUCCESS;
     const std::array<int, 9> key = {op->g.L[0], op->g.L[1], op->g.L[2], op->g.L[3], op->g.nd,
                                     op->prec,   op->recon,  op->nrhs,   op->format};
     {
@@ -266,7 +276,9 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     std::vector<std::array<int, 3>> cand;
     if (generic(op)) {
-        cand = {{op->block, op->variant, 0}, {op->block, op->variant, 1}};
+        cand = {{op->block, 0, 0}};
+        if (v2ok) cand.push_back({op->block, 1, 0});
+        if (tc_eligible(op)) cand.push_back({op->block, 0, 1});
     } else {
         cand = {{64, 0, 0}, {128, 0, 0}, {256, 0, 0}};
         for (int v = 1; v < dslash_variants(op->prec); v++) cand.push_back({128, v, 0});
@@ -378,9 +390,10 @@ extern "C" int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, vo
     }
     if (generic(op)) {
         cudaError_t e = op->format == GBDS_SPINOR_NATIVE
-                            ? launch_gen_f32(op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f, nullptr, s)
+                            ? launch_gen_f32(op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f, nullptr, s,
+                                             op->variant)
                             : launch_gen_half(op->format, op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr,
-                                              0.f, nullptr, s);
+                                              0.f, nullptr, s, op->variant);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
     }
     cudaError_t e = op->prec == 32 ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)

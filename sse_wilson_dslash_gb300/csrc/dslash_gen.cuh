@@ -228,6 +228,119 @@ __device__ __forceinline__ void block_sum_rhs(double *partials, float v) {
             ws[0][threadIdx.x] + ws[1][threadIdx.x] + ws[2][threadIdx.x] + ws[3][threadIdx.x];
 }
 
+// ---------------------------------------------------------------------------
+// Variant with the colour multiply in packed FP32x2 arithmetic (NRHS 8..32,
+// FP32 links): each CTA first stages the eight links of each of its sites in
+// shared memory as splats (Mr, Mr, -Mi, Mi) of M = U (forward hop) or
+// M = U^dagger (backward hop), so that
+//   w_i = sum_j (Mr, Mr) * (hr, hi) + (-Mi, Mi) * (hi, hr)
+// is two __ffma2_rn per complex multiply-add with no operand moves; the nrhs
+// threads of a site read each staged entry as a shared-memory broadcast.
+// ---------------------------------------------------------------------------
+
+// w_k = M h_k (k = 0, 1) from the staged splats M[i*3 + j]
+__device__ __forceinline__ void su3_mul_splat(const float4 *M, const cx<float> (&h)[2][3], cx<float> (&w)[2][3]) {
+    float2 hv[2][3], hs[2][3];
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            hv[k][j] = make_float2(h[k][j].r, h[k][j].i);
+            hs[k][j] = make_float2(h[k][j].i, h[k][j].r);
+        }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float2 w0 = make_float2(0.f, 0.f), w1 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const float4 m = M[i * 3 + j];
+            const float2 a = make_float2(m.x, m.y), b = make_float2(m.z, m.w);
+            w0 = __ffma2_rn(a, hv[0][j], w0);
+            w0 = __ffma2_rn(b, hs[0][j], w0);
+            w1 = __ffma2_rn(a, hv[1][j], w1);
+            w1 = __ffma2_rn(b, hs[1][j], w1);
+        }
+        w[0][i] = {w0.x, w0.y};
+        w[1][i] = {w1.x, w1.y};
+    }
+}
+
+template <int FMT, int RECON, int ISIGN, int NRHS, int EPI>
+__global__ void __launch_bounds__(128, 6) dslash_gen2_kernel(const GenArgs a) {
+    static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
+    constexpr int P = 128 / NRHS;  // sites per CTA
+    __shared__ float4 sL[P][8][9];
+    const int t = threadIdx.x;
+    const int p = t / NRHS, r = t % NRHS;
+    const int h = blockIdx.x * P + p;
+    const bool act = h < a.g.Vh;
+    Nbr n;
+    if (act) neighbours<4>(a.g, h, a.pt, n);
+    if (act && r < 8) {
+        // link r of the site: direction r / 2, forward (even r) or backward
+        const int mu = r >> 1;
+        const bool bwd = r & 1;
+        const int nbm = mu == 0 ? n.b[0] : (mu == 1 ? n.b[1] : (mu == 2 ? n.b[2] : n.b[3]));
+        const int lp = bwd ? 1 - a.pt : a.pt;
+        cx<float> U[3][3];
+        Field<float>::template load_link<RECON>(a.gauge + (size_t)(lp * 4 + mu) * a.link_block_bytes, a.g.stride,
+                                                bwd ? nbm : h, U);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                // forward: M_ij = U_ij; backward: M_ij = conj(U_ji)
+                const float mr = bwd ? U[j][i].r : U[i][j].r;
+                const float mi = bwd ? -U[j][i].i : U[i][j].i;
+                sL[p][r][i * 3 + j] = make_float4(mr, mr, -mi, mi);
+            }
+    }
+    __syncthreads();
+    float nrm = 0.f;
+    if (act) {
+        cx<float> acc[4][3];
+#pragma unroll
+        for (int s = 0; s < 4; s++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) acc[s][c] = {0.f, 0.f};
+#define GBDS_G2_HOP(MU)                                                              \
+    {                                                                                \
+        cx<float> sp[4][3], hs[2][3], w[2][3];                                       \
+        Sio<FMT>::load(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, sp);                 \
+        project<MU, ISIGN>(sp, hs);                                                  \
+        su3_mul_splat(sL[p][2 * MU], hs, w);                                         \
+        reconstruct<MU, ISIGN>(acc, w);                                              \
+        Sio<FMT>::load(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, sp);                 \
+        project<MU, -ISIGN>(sp, hs);                                                 \
+        su3_mul_splat(sL[p][2 * MU + 1], hs, w);                                     \
+        reconstruct<MU, -ISIGN>(acc, w);                                             \
+    }
+        GBDS_G2_HOP(0)
+        GBDS_G2_HOP(1)
+        GBDS_G2_HOP(2)
+        GBDS_G2_HOP(3)
+#undef GBDS_G2_HOP
+        const size_t i = (size_t)h * NRHS + r;
+        if constexpr (EPI) {
+            cx<float> xv[4][3];
+            Sio<FMT>::load(a.x, a.cs, i, xv);
+#pragma unroll
+            for (int s = 0; s < 4; s++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    acc[s][c].r = fmaf(a.coef, acc[s][c].r, xv[s][c].r);
+                    acc[s][c].i = fmaf(a.coef, acc[s][c].i, xv[s][c].i);
+                    nrm = fmaf(acc[s][c].r, acc[s][c].r, nrm);
+                    nrm = fmaf(acc[s][c].i, acc[s][c].i, nrm);
+                }
+        }
+        Sio<FMT>::store(a.res, a.cs, i, acc);
+    }
+    if constexpr (EPI == 2) {
+        if (a.partials) block_sum_rhs<NRHS>(a.partials, nrm);
+    }
+}
+
 // One thread per (site, rhs); 4D.  EPI = 1 adds the xpay epilogue
 // (res = x + coef * D psi) with one |res|^2 partial per block; EPI = 2 the
 // same with one partial per block and rhs (NRHS 2..32, 128-thread blocks).

@@ -3,8 +3,8 @@
 
 namespace gbds {
 cudaError_t launch_gen_f32(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
-                           int cb, const void *x, float coef, double *partials, cudaStream_t st) {
-    return launch_gen_t<kFmtNative>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st);
+                           int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant) {
+    return launch_gen_t<kFmtNative>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st, variant);
 }
 cudaError_t launch_pack_gen_f32(const Geom &g, int nrhs, const float *packed, const int *table, int parity, void *out,
                                 cudaStream_t st) {

@@ -4,9 +4,10 @@
 
 namespace gbds {
 cudaError_t launch_gen_half(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,
-                            int isign, int cb, const void *x, float coef, double *partials, cudaStream_t st) {
-    if (fmt == kFmtBF16) return launch_gen_t<kFmtBF16>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st);
-    return launch_gen_t<kFmtF16N>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st);
+                            int isign, int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant) {
+    if (fmt == kFmtBF16)
+        return launch_gen_t<kFmtBF16>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st, variant);
+    return launch_gen_t<kFmtF16N>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st, variant);
 }
 cudaError_t launch_gen_h16(int fmt, const Geom &g, int recon, const void *gauge, const void *psi, void *res, int isign,
                            int cb, const void *x, float coef, double *partials, cudaStream_t st) {

@@ -86,9 +86,19 @@ cudaError_t launch_gen_h16_t(const Geom &g, int recon, const void *gauge, const 
     return cudaGetLastError();
 }
 
+template <int FMT, int RECON, int ISIGN, int EPI>
+void launch_gen2_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
+    const unsigned vh = (unsigned)a.g.Vh;
+    switch (nrhs) {
+    case 8: dslash_gen2_kernel<FMT, RECON, ISIGN, 8, EPI><<<(vh + 15) / 16, 128, 0, st>>>(a); break;
+    case 16: dslash_gen2_kernel<FMT, RECON, ISIGN, 16, EPI><<<(vh + 7) / 8, 128, 0, st>>>(a); break;
+    default: dslash_gen2_kernel<FMT, RECON, ISIGN, 32, EPI><<<(vh + 3) / 4, 128, 0, st>>>(a); break;
+    }
+}
+
 template <int FMT>
 cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
-                         int cb, const void *x, float coef, double *partials, cudaStream_t st) {
+                         int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0) {
     GenArgs a;
     a.g = g;
     a.psi = static_cast<const char *>(psi);
@@ -106,9 +116,12 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     const bool epi = x != nullptr;
     // the xpay epilogue takes nrhs 1 or a power of two up to 32
     if (epi && (nrhs > 32 || (nrhs & (nrhs - 1)) != 0)) return cudaErrorInvalidValue;
+    const bool v2 = variant == 1 && (nrhs == 8 || nrhs == 16 || nrhs == 32);
 #define GBDS_GEN(R, S)                                                   \
     do {                                                                 \
-        if (epi && nrhs == 1) launch_gen_nrhs<FMT, R, S, 1>(a, nrhs, grid, st);  \
+        if (v2 && epi) launch_gen2_nrhs<FMT, R, S, 2>(a, nrhs, st);      \
+        else if (v2) launch_gen2_nrhs<FMT, R, S, 0>(a, nrhs, st);        \
+        else if (epi && nrhs == 1) launch_gen_nrhs<FMT, R, S, 1>(a, nrhs, grid, st);  \
         else if (epi) launch_gen_nrhs<FMT, R, S, 2>(a, nrhs, grid, st);  \
         else launch_gen_nrhs<FMT, R, S, 0>(a, nrhs, grid, st);           \
     } while (0)

@@ -56,10 +56,12 @@ cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_
 // {1,2,4,8,16,32}, spinor formats 0 FP32, 1 BF16, 2 FP16 + norm.  x != nullptr
 // selects the xpay epilogue res = x + coef * D psi (nrhs 1 only) with |res|^2
 // partials per 128-thread block.
+// variant 1: the colour multiply in packed FP32x2 arithmetic on links staged
+// per CTA (nrhs 8, 16, 32; other counts take variant 0).
 cudaError_t launch_gen_f32(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
-                           int cb, const void *x, float coef, double *partials, cudaStream_t st);
+                           int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0);
 cudaError_t launch_gen_half(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,
-                            int isign, int cb, const void *x, float coef, double *partials, cudaStream_t st);
+                            int isign, int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0);
 // packed: FP32 [nrhs][V][4][3][2], caller order
 cudaError_t launch_pack_gen_f32(const Geom &g, int nrhs, const float *packed, const int *table, int parity, void *out,
                                 cudaStream_t st);
