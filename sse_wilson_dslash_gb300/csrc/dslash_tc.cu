@@ -36,6 +36,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "dslash_gen.cuh"
@@ -582,24 +583,33 @@ template <int FMT, int RECON, int ISIGN, int NRHS>
 cudaError_t launch_tc_t(TcArgs a, cudaStream_t st) {
     using S = TcShape<NRHS>;
     auto k = dslash_tc_kernel<FMT, RECON, ISIGN, NRHS>;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, k);
+    // resident CTAs per SM, per device (computed once): 64K registers
+    // (allocated per warp in steps of 256), 228 KB of shared memory (1 KB
+    // reserved per CTA), 2048 threads, and the 512 TMEM columns
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> resident[kMaxDev];  // SMs x CTAs per SM; 0 = not yet known
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    // resident CTAs per SM: 64K registers (allocated per warp in steps of
-    // 256), 228 KB of shared memory (1 KB reserved per CTA), 2048 threads,
-    // and the 512 TMEM columns
-    const int regs = ((fa.numRegs * 32 + 255) / 256) * 256 * 4;
-    int occ = 65536 / (regs > 0 ? regs : 1);
-    const int by_smem = (228 * 1024) / ((int)fa.sharedSizeBytes + 1024);
-    occ = occ < by_smem ? occ : by_smem;
-    occ = occ < 16 ? occ : 16;
-    occ = occ < 512 / S::COLS ? occ : 512 / S::COLS;
-    occ = occ < 1 ? 1 : occ;
+    int slots = (dev >= 0 && dev < kMaxDev) ? resident[dev].load() : 0;
+    if (slots == 0) {
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncAttributes fa;
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k);
+        if (e != cudaSuccess) return e;
+        const int regs = ((fa.numRegs * 32 + 255) / 256) * 256 * 4;
+        int occ = 65536 / (regs > 0 ? regs : 1);
+        const int by_smem = (228 * 1024) / ((int)fa.sharedSizeBytes + 1024);
+        occ = occ < by_smem ? occ : by_smem;
+        occ = occ < 16 ? occ : 16;
+        occ = occ < 512 / S::COLS ? occ : 512 / S::COLS;
+        occ = occ < 1 ? 1 : occ;
+        slots = sms * occ;
+        if (dev >= 0 && dev < kMaxDev) resident[dev].store(slots);
+    }
     a.ntiles = (a.g.Vh + S::P - 1) / S::P;
-    const int grid = a.ntiles < sms * occ ? a.ntiles : sms * occ;
+    const int grid = a.ntiles < slots ? a.ntiles : slots;
     k<<<grid, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
