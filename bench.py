@@ -53,6 +53,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_time_max(ms_total, world, device):
+    """The slowest rank's timed-region duration: each rank runs one replica of
+    the same workload, so the job takes as long as its slowest replica."""
+    if world <= 1:
+        return ms_total
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_total], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_gflops(ms_total, world, sites, steps):
+    """Whole-job GFLOP/s: all replicas' output sites over the slowest time."""
+    return FLOPS_4D * sites * steps * world / (ms_total * 1e6)
+
+
 # ---------------------------------------------------------------------------
 # Clock sampling (nvidia-smi during the timed region)
 # ---------------------------------------------------------------------------
@@ -554,15 +571,10 @@ def run_gb300(args):
     barrier()
     t_wall1 = time.time()
     launches = _lib.launch_count() - launches0
-    ms_total = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = replica_time_max(e0.elapsed_time(e1), world, "cuda")
     ms = ms_total / args.steps
     sites = op.volume_cb
-    value = FLOPS_4D * sites * args.steps * world / (ms_total * 1e6)
+    value = replica_gflops(ms_total, world, sites, args.steps)
     bytes_per_site = op.bytes_per_site
     achieved = bytes_per_site * sites / (ms * 1e6)
     # Keep the clock sampler running a little longer to cover short regions.
