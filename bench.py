@@ -312,7 +312,7 @@ def multi_rhs_variants(torch, steps, peak):
             gbs = op.bytes_per_site * sites / (ms * 1e6)
             out[f"{'f32' if fmt == 'native' else 'bf16'}_nrhs{nrhs}"] = {
                 "ms": ms, "gflops": 1320 * sites / (ms * 1e6), "gbs": gbs, "roofline_frac": gbs / peak,
-                "ms_per_rhs": ms / nrhs, "bytes_per_site_rhs": op.bytes_per_site}
+                "ms_per_rhs": ms / nrhs, "bytes_per_site_rhs": op.bytes_per_site, "variant": op.tuning()[1]}
             del gauge, srcs, outs
             op.close()
             torch.cuda.empty_cache()
@@ -338,7 +338,8 @@ def multi_rhs_variants(torch, steps, peak):
                 sites = op.volume_cb * nrhs
                 gbs = op.bytes_per_site * sites / (ms * 1e6)
                 out[key] = {"ms": ms, "gflops": 1320 * sites / (ms * 1e6), "gbs": gbs, "roofline_frac": gbs / peak,
-                            "ms_per_rhs": ms / nrhs, "bytes_per_site_rhs": op.bytes_per_site}
+                            "ms_per_rhs": ms / nrhs, "bytes_per_site_rhs": op.bytes_per_site,
+                            "variant": "tc" if tc else op.tuning()[1]}
                 del gauge, srcs, outs
                 op.close()
                 torch.cuda.empty_cache()

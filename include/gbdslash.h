@@ -150,8 +150,10 @@ int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
  * uncapped; 1.. = variants that cap registers for more resident warps, which
  * launch 128-thread blocks.  Several rhs or 16-bit storage: 0 = the plain
  * multi-RHS kernel, 1 = the packed FP32x2 form (8, 16, 32 rhs; the block
- * size is fixed at 128).  gbds_op_num_variants gives the count.  Used by the
- * autotuner. */
+ * size is fixed at 128), and for 16-bit storage 2 = projection, multiply and
+ * reconstruction all in packed FP32x2 (8, 16, 32 rhs; 128-thread blocks).
+ * Variants 1 and 2 run the plain kernel for other counts of rhs.
+ * gbds_op_num_variants gives the count.  Used by the autotuner. */
 int gbds_op_set_tuning(gbds_op op, int threads, int variant);
 int gbds_op_get_tuning(gbds_op op, int *threads, int *variant);
 int gbds_op_num_variants(gbds_op op);
@@ -160,11 +162,11 @@ int gbds_op_num_variants(gbds_op op);
  * fields (res is overwritten), keep the fastest for this operator and cache
  * it process-wide for its (dims, nd, prec, recon, nrhs, format); a later call
  * for the same shape takes the cached choice without timing.  Operators with
- * several right-hand sides (or 16-bit storage) have two variants: 0 the plain
- * multi-RHS kernel, 1 the colour multiply in packed FP32x2 arithmetic on
- * links staged per CTA (8, 16 or 32 rhs); for 16-bit formats with 16 or 32
- * rhs the tensor-core kernel (gbds_op_set_tensor_cores) is a third
- * candidate.  Synchronises `stream`. */
+ * several right-hand sides (or 16-bit storage) have these candidates: 0 the
+ * plain multi-RHS kernel, 1 the colour multiply in packed FP32x2 arithmetic
+ * on links staged per CTA (8, 16 or 32 rhs), for 16-bit formats 2 the whole
+ * hop in packed FP32x2 (8, 16, 32 rhs) and with 16 or 32 rhs the
+ * tensor-core kernel (gbds_op_set_tensor_cores).  Synchronises `stream`. */
 int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream);
 
 /* Number of kernels this library has launched in this process (all kinds). */

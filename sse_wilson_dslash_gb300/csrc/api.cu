@@ -120,10 +120,12 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     o->format = format;
     // Single rhs: the register-cap variant (see above).  Several rhs or
     // 16-bit storage: variant 0 = the plain multi-RHS kernel, 1 = its packed
-    // FP32x2 form (nrhs 8, 16, 32), measured faster from 16 rhs on at
-    // 24^3x48 (autotune chooses per shape).
+    // FP32x2 colour multiply, 2 = the whole hop packed (16-bit storage); from
+    // 16 rhs on (at 24^3x48) 2 is fastest for 16-bit storage and 1 for FP32
+    // (autotune chooses per shape).
     const bool gen = nrhs > 1 || format != GBDS_SPINOR_NATIVE;
-    o->variant = gen ? (nrhs >= 16 ? 1 : 0) : ((prec == 32 && recon == 18) ? 1 : 0);
+    const int gen_variant = nrhs >= 16 ? (format != GBDS_SPINOR_NATIVE ? 2 : 1) : 0;
+    o->variant = gen ? gen_variant : ((prec == 32 && recon == 18) ? 1 : 0);
     o->tensor_cores = 0;
     o->d_err = nullptr;
     o->d_site_table = nullptr;
@@ -242,7 +244,8 @@ extern "C" int gbds_op_set_tuning(gbds_op op, int threads, int variant) {
 
 extern "C" int gbds_op_num_variants(gbds_op op) {
     if (!op) return 0;
-    return (op->nrhs > 1 || op->format != GBDS_SPINOR_NATIVE) ? 2 : dslash_variants(op->prec);
+    if (op->format != GBDS_SPINOR_NATIVE) return 3;  // + the fully packed 16-bit kernel
+    return op->nrhs > 1 ? 2 : dslash_variants(op->prec);
 }
 
 namespace {
@@ -278,6 +281,7 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
     if (generic(op)) {
         cand = {{op->block, 0, 0}};
         if (v2ok) cand.push_back({op->block, 1, 0});
+        if (v2ok && op->format != GBDS_SPINOR_NATIVE) cand.push_back({op->block, 2, 0});
         if (tc_eligible(op)) cand.push_back({op->block, 0, 1});
     } else {
         cand = {{64, 0, 0}, {128, 0, 0}, {256, 0, 0}};

@@ -20,6 +20,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "dslash_kernel.cuh"
 
 namespace gbds {
@@ -239,6 +241,58 @@ __device__ __forceinline__ void block_sum_rhs(double *partials, float v) {
 // ---------------------------------------------------------------------------
 
 // w_k = M h_k (k = 0, 1) from the staged splats M[i*3 + j]
+// a + code * b on one complex held as an (r, i) pair: one packed FP32x2
+// operation for a real coefficient (+1, -1); the imaginary ones (+i, -i)
+// would need b's parts swapped, so they stay scalar.
+template <int CODE>
+__device__ __forceinline__ cx<float> cadd_code(cx<float> a, cx<float> b) {
+    if constexpr (CODE >= 2) {
+        return cadd(a, mulc<CODE>(b));
+    } else {
+        const float2 v = CODE == 0 ? __fadd2_rn(make_float2(a.r, a.i), make_float2(b.r, b.i))
+                                   : __ffma2_rn(make_float2(b.r, b.i), make_float2(-1.f, -1.f), make_float2(a.r, a.i));
+        return {v.x, v.y};
+    }
+}
+
+template <int MU, int SIGMA>
+__device__ __forceinline__ void project_pairs(const cx<float> (&s)[4][3], cx<float> (&h)[2][3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIGMA > 0 ? 0 : 1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        h[0][c] = cadd_code<P::a0 ^ f>(s[0][c], s[P::j0][c]);
+        h[1][c] = cadd_code<P::a1 ^ f>(s[1][c], s[P::j1][c]);
+    }
+}
+
+template <int MU, int SIGMA>
+__device__ __forceinline__ void reconstruct_pairs(cx<float> (&acc)[4][3], const cx<float> (&w)[2][3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIGMA > 0 ? 0 : 1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        acc[0][c] = cadd_code<0>(acc[0][c], w[0][c]);
+        acc[1][c] = cadd_code<0>(acc[1][c], w[1][c]);
+        acc[2][c] = cadd_code<P::b2 ^ f>(acc[2][c], w[P::k2][c]);
+        acc[3][c] = cadd_code<P::b3 ^ f>(acc[3][c], w[P::k3][c]);
+    }
+}
+
+// Variant 1's projection and reconstruction: in pairs for 16-bit storage
+// (measured faster), scalar for FP32 storage (measured slower in pairs).
+template <int FMT, int MU, int SIGMA>
+__device__ __forceinline__ void g2_project(const cx<float> (&s)[4][3], cx<float> (&h)[2][3]) {
+    if constexpr (FMT == kFmtNative) project<MU, SIGMA>(s, h);
+    else project_pairs<MU, SIGMA>(s, h);
+}
+
+template <int FMT, int MU, int SIGMA>
+__device__ __forceinline__ void g2_reconstruct(cx<float> (&acc)[4][3], const cx<float> (&w)[2][3]) {
+    if constexpr (FMT == kFmtNative) reconstruct<MU, SIGMA>(acc, w);
+    else reconstruct_pairs<MU, SIGMA>(acc, w);
+}
+
 __device__ __forceinline__ void su3_mul_splat(const float4 *M, const cx<float> (&h)[2][3], cx<float> (&w)[2][3]) {
     float2 hv[2][3], hs[2][3];
 #pragma unroll
@@ -307,13 +361,13 @@ __global__ void __launch_bounds__(128, 6) dslash_gen2_kernel(const GenArgs a) {
     {                                                                                \
         cx<float> sp[4][3], hs[2][3], w[2][3];                                       \
         Sio<FMT>::load(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, sp);                 \
-        project<MU, ISIGN>(sp, hs);                                                  \
+        g2_project<FMT, MU, ISIGN>(sp, hs);                                          \
         su3_mul_splat(sL[p][2 * MU], hs, w);                                         \
-        reconstruct<MU, ISIGN>(acc, w);                                              \
+        g2_reconstruct<FMT, MU, ISIGN>(acc, w);                                      \
         Sio<FMT>::load(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, sp);                 \
-        project<MU, -ISIGN>(sp, hs);                                                 \
+        g2_project<FMT, MU, -ISIGN>(sp, hs);                                         \
         su3_mul_splat(sL[p][2 * MU + 1], hs, w);                                     \
-        reconstruct<MU, -ISIGN>(acc, w);                                             \
+        g2_reconstruct<FMT, MU, -ISIGN>(acc, w);                                     \
     }
         GBDS_G2_HOP(0)
         GBDS_G2_HOP(1)
@@ -338,6 +392,172 @@ __global__ void __launch_bounds__(128, 6) dslash_gen2_kernel(const GenArgs a) {
     }
     if constexpr (EPI == 2) {
         if (a.partials) block_sum_rhs<NRHS>(a.partials, nrm);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fully packed variant for 16-bit spinors (BF16, half + norm), NRHS 8..32:
+// projection, colour multiply and reconstruction all run on pairs holding
+// the same part (real or imaginary) of the two spin halves,
+//   R_c = (h0_c.r, h1_c.r),  I_c = (h0_c.i, h1_c.i),
+// one __ffma2_rn / __fadd2_rn per two reals and no operand moves: the
+// 16-bit -> FP32 conversion writes each value straight into its pair.
+//   projection  R_c = (s0_c.r, s1_c.r) + (g0, g1) * (part of s_j0_c, s_j1_c)
+//   multiply    W_R = sum_j Mr R_j - Mi I_j,   W_I = sum_j Mr I_j + Mi R_j
+//   upper       (acc0, acc1) += W
+//   lower       (acc2, acc3) += (b2 w0, b3 w1) for mu = 2, 3 (k2, k3 = 0, 1)
+//               (acc3, acc2) += (b3 w0, b2 w1) for mu = 0, 1 (k2, k3 = 1, 0)
+// The lower pairs change order once, between mu = 1 and mu = 2.  Links are
+// staged in shared memory as (Mr, Mr, Mi, Mi) of M = U or U^dagger.
+// ---------------------------------------------------------------------------
+
+// Re and Im of (code * s) in terms of the parts of s: code 0 (+1): (+r, +i),
+// 1 (-1): (-r, -i), 2 (+i): (-i, +r), 3 (-i): (+i, -r).
+template <int CODE>
+struct CPart {
+    static constexpr bool swap = CODE >= 2;  // the real part comes from s.i
+    static constexpr float sre = (CODE == 0 || CODE == 3) ? 1.f : -1.f;
+    static constexpr float sim = (CODE == 0 || CODE == 2) ? 1.f : -1.f;
+};
+
+// the 24 reals of a stored 16-bit spinor, (s[j/3][j%3].r, .i) at 2j, 2j+1;
+// returns the scale (the norm of half + norm, 1 for BF16)
+template <int FMT>
+__device__ __forceinline__ float load_reals16(const char *base, size_t cs, size_t i, float (&v)[24]) {
+    static_assert(FMT == kFmtBF16 || FMT == kFmtF16N, "16-bit formats");
+    const uint4 *p = reinterpret_cast<const uint4 *>(base);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint4 q = __ldg(p + k * cs + i);
+        const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            if constexpr (FMT == kFmtBF16) {
+                v[8 * k + 2 * c] = __uint_as_float(w[c] << 16);
+                v[8 * k + 2 * c + 1] = __uint_as_float(w[c] & 0xffff0000u);
+            } else {
+                const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[c]));
+                v[8 * k + 2 * c] = f.x;
+                v[8 * k + 2 * c + 1] = f.y;
+            }
+        }
+    }
+    if constexpr (FMT == kFmtF16N) return __ldg(Sio<kFmtF16N>::norms(base, cs) + i);
+    else return 1.f;
+}
+
+// One hop: project v (scaled by nrm for half + norm), multiply by the staged
+// M, add into the upper pairs U and the lower pairs L (order LORD: 0 =
+// (acc2, acc3), 1 = (acc3, acc2)).
+template <int MU, int SIG, int LORD, bool SCALE>
+__device__ __forceinline__ void packed_hop(const float (&v)[24], float nrm, const float4 *M, float2 (&UR)[3],
+                                           float2 (&UI)[3], float2 (&LR)[3], float2 (&LI)[3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIG > 0 ? 0 : 1;
+    using A0 = CPart<P::a0 ^ f>;
+    using A1 = CPart<P::a1 ^ f>;
+    using B2 = CPart<P::b2 ^ f>;
+    using B3 = CPart<P::b3 ^ f>;
+    static_assert(A0::swap == A1::swap && B2::swap == B3::swap, "both halves take the same parts");
+    static_assert(LORD == 0 ? (P::k2 == 0 && P::k3 == 1) : (P::k2 == 1 && P::k3 == 0), "lower pair order");
+    float2 R[3], I[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int s0 = 2 * c, s1 = 2 * (3 + c), j0 = 2 * (3 * P::j0 + c), j1 = 2 * (3 * P::j1 + c);
+        R[c] = __ffma2_rn(make_float2(v[j0 + (A0::swap ? 1 : 0)], v[j1 + (A1::swap ? 1 : 0)]),
+                          make_float2(A0::sre, A1::sre), make_float2(v[s0], v[s1]));
+        I[c] = __ffma2_rn(make_float2(v[j0 + (A0::swap ? 0 : 1)], v[j1 + (A1::swap ? 0 : 1)]),
+                          make_float2(A0::sim, A1::sim), make_float2(v[s0 + 1], v[s1 + 1]));
+        if constexpr (SCALE) {
+            R[c] = __fmul2_rn(R[c], make_float2(nrm, nrm));
+            I[c] = __fmul2_rn(I[c], make_float2(nrm, nrm));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float2 ar = make_float2(0.f, 0.f), br = make_float2(0.f, 0.f), ai = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const float4 m = M[i * 3 + j];
+            const float2 mr = make_float2(m.x, m.y), mi = make_float2(m.z, m.w);
+            ar = __ffma2_rn(mr, R[j], ar);
+            br = __ffma2_rn(mi, I[j], br);
+            ai = __ffma2_rn(mr, I[j], ai);
+            ai = __ffma2_rn(mi, R[j], ai);
+        }
+        const float2 wr = __ffma2_rn(br, make_float2(-1.f, -1.f), ar);
+        UR[i] = __fadd2_rn(UR[i], wr);
+        UI[i] = __fadd2_rn(UI[i], ai);
+        using X = std::conditional_t<LORD == 0, B2, B3>;  // first element of the lower pair
+        using Y = std::conditional_t<LORD == 0, B3, B2>;
+        LR[i] = __ffma2_rn(B2::swap ? ai : wr, make_float2(X::sre, Y::sre), LR[i]);
+        LI[i] = __ffma2_rn(B2::swap ? wr : ai, make_float2(X::sim, Y::sim), LI[i]);
+    }
+}
+
+template <int FMT, int RECON, int ISIGN, int NRHS>
+__global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
+    static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
+    constexpr int P = 128 / NRHS;  // sites per CTA
+    constexpr bool SCALE = FMT == kFmtF16N;
+    __shared__ float4 sL[P][8][9];
+    const int t = threadIdx.x;
+    const int p = t / NRHS, r = t % NRHS;
+    const int h = blockIdx.x * P + p;
+    const bool act = h < a.g.Vh;
+    Nbr n;
+    if (act) neighbours<4>(a.g, h, a.pt, n);
+    if (act && r < 8) {
+        // link r of the site: direction r / 2, forward (even r) or backward
+        const int mu = r >> 1;
+        const bool bwd = r & 1;
+        const int nbm = mu == 0 ? n.b[0] : (mu == 1 ? n.b[1] : (mu == 2 ? n.b[2] : n.b[3]));
+        const int lp = bwd ? 1 - a.pt : a.pt;
+        cx<float> U[3][3];
+        Field<float>::template load_link<RECON>(a.gauge + (size_t)(lp * 4 + mu) * a.link_block_bytes, a.g.stride,
+                                                bwd ? nbm : h, U);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                // forward: M_ij = U_ij; backward: M_ij = conj(U_ji)
+                const float mr = bwd ? U[j][i].r : U[i][j].r;
+                const float mi = bwd ? -U[j][i].i : U[i][j].i;
+                sL[p][r][i * 3 + j] = make_float4(mr, mr, mi, mi);
+            }
+    }
+    __syncthreads();
+    if (act) {
+        float2 UR[3], UI[3], LR[3], LI[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) UR[c] = UI[c] = LR[c] = LI[c] = make_float2(0.f, 0.f);
+#define GBDS_G3_HOP(MU, LORD)                                                                            \
+    {                                                                                                    \
+        float v[24];                                                                                     \
+        float sc = load_reals16<FMT>(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, v);                        \
+        packed_hop<MU, ISIGN, LORD, SCALE>(v, sc, sL[p][2 * MU], UR, UI, LR, LI);                        \
+        sc = load_reals16<FMT>(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, v);                              \
+        packed_hop<MU, -ISIGN, LORD, SCALE>(v, sc, sL[p][2 * MU + 1], UR, UI, LR, LI);                   \
+    }
+        GBDS_G3_HOP(0, 1)
+        GBDS_G3_HOP(1, 1)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            LR[c] = make_float2(LR[c].y, LR[c].x);
+            LI[c] = make_float2(LI[c].y, LI[c].x);
+        }
+        GBDS_G3_HOP(2, 0)
+        GBDS_G3_HOP(3, 0)
+#undef GBDS_G3_HOP
+        cx<float> acc[4][3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            acc[0][c] = {UR[c].x, UI[c].x};
+            acc[1][c] = {UR[c].y, UI[c].y};
+            acc[2][c] = {LR[c].x, LI[c].x};
+            acc[3][c] = {LR[c].y, LI[c].y};
+        }
+        Sio<FMT>::store(a.res, a.cs, (size_t)h * NRHS + r, acc);
     }
 }
 

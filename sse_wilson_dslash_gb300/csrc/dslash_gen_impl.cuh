@@ -96,6 +96,16 @@ void launch_gen2_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
     }
 }
 
+template <int FMT, int RECON, int ISIGN>
+void launch_gen3_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
+    const unsigned vh = (unsigned)a.g.Vh;
+    switch (nrhs) {
+    case 8: dslash_gen3_kernel<FMT, RECON, ISIGN, 8><<<(vh + 15) / 16, 128, 0, st>>>(a); break;
+    case 16: dslash_gen3_kernel<FMT, RECON, ISIGN, 16><<<(vh + 7) / 8, 128, 0, st>>>(a); break;
+    default: dslash_gen3_kernel<FMT, RECON, ISIGN, 32><<<(vh + 3) / 4, 128, 0, st>>>(a); break;
+    }
+}
+
 template <int FMT>
 cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
                          int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0) {
@@ -116,9 +126,19 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     const bool epi = x != nullptr;
     // the xpay epilogue takes nrhs 1 or a power of two up to 32
     if (epi && (nrhs > 32 || (nrhs & (nrhs - 1)) != 0)) return cudaErrorInvalidValue;
-    const bool v2 = variant == 1 && (nrhs == 8 || nrhs == 16 || nrhs == 32);
+    const bool packed_nrhs = nrhs == 8 || nrhs == 16 || nrhs == 32;
+    const bool v2 = variant == 1 && packed_nrhs;
+    // variant 2 (fully packed, no epilogue) exists for the 16-bit formats;
+    // like variant 1, it falls back to the plain kernel otherwise
+    const bool v3 = variant == 2 && packed_nrhs && FMT != kFmtNative && !epi;
 #define GBDS_GEN(R, S)                                                   \
     do {                                                                 \
+        if constexpr (FMT != kFmtNative) {                               \
+            if (v3) {                                                    \
+                launch_gen3_nrhs<FMT, R, S>(a, nrhs, st);                \
+                break;                                                   \
+            }                                                            \
+        }                                                                \
         if (v2 && epi) launch_gen2_nrhs<FMT, R, S, 2>(a, nrhs, st);      \
         else if (v2) launch_gen2_nrhs<FMT, R, S, 0>(a, nrhs, st);        \
         else if (epi && nrhs == 1) launch_gen_nrhs<FMT, R, S, 1>(a, nrhs, grid, st);  \

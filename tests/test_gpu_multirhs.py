@@ -221,7 +221,8 @@ def test_tensor_core_production_lattice():
 @pytest.mark.parametrize("nrhs", [8, 16, 32])
 def test_packed_fp32x2_variant_matches_oracle(nrhs, fmt):
     """Variant 1 of the multi-RHS kernel (links staged per CTA, colour
-    multiply in packed FP32x2 arithmetic) against the oracle."""
+    multiply in packed FP32x2 arithmetic) and, for 16-bit storage, variant 2
+    (the whole hop in packed FP32x2) against the oracle."""
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
     dims = (8, 4, 6, 4)
@@ -230,10 +231,11 @@ def test_packed_fp32x2_variant_matches_oracle(nrhs, fmt):
     rng = np.random.default_rng(300 + nrhs)
     u = O.random_gauge(rng, V)
     psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
-    for recon in (18, 12):
+    variants = (1,) if fmt == "native" else (1, 2)
+    for recon, variant in [(rc, v) for rc in (18, 12) for v in variants]:
         op = DslashOperator(dims, nd=4, prec=32, recon=recon, nrhs=nrhs, spinor_format=fmt)
-        assert op.num_variants == 2
-        op.set_tuning(0, 1)
+        assert op.num_variants == (2 if fmt == "native" else 3)
+        op.set_tuning(0, variant)
         gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
         packed = torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda()
         for isign, cb in ((1, 0), (-1, 1)):
@@ -244,5 +246,5 @@ def test_packed_fp32x2_variant_matches_oracle(nrhs, fmt):
             ts = O.target_sites(4, dims, lol, cb)
             for r in range(nrhs):
                 ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
-                assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt], (recon, isign, cb, r)
+                assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt], (recon, variant, isign, cb, r)
         op.close()
