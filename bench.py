@@ -290,17 +290,18 @@ def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None):
 
 
 def multi_rhs_variants(torch, steps, peak):
-    """Several right-hand sides on one 24^3x48 gauge field: FP32 and BF16
-    spinor storage, 18-real links; GFLOP/s counts 1320 flop per site and
-    right-hand side."""
+    """Several right-hand sides on one 24^3x48 gauge field: FP32, FP32 in
+    spin pairs and BF16 spinor storage, 18-real links; GFLOP/s counts 1320
+    flop per site and right-hand side."""
     from sse_wilson_dslash_gb300.device import DslashOperator
     dims = (24, 24, 24, 48)
     V = dims[0] * dims[1] * dims[2] * dims[3]
     gen = torch.Generator(device="cuda").manual_seed(7)
     u = su3_links(V * 4, gen, torch).float().reshape(-1)
     out = {}
-    for fmt in ("native", "bf16"):
-        for nrhs in (1, 4, 8, 16, 32):
+    names = {"native": "f32", "f32_pairs": "f32pairs", "bf16": "bf16"}
+    for fmt, counts in (("native", (1, 4, 8, 16, 32)), ("f32_pairs", (16, 32)), ("bf16", (1, 4, 8, 16, 32))):
+        for nrhs in counts:
             op = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
             gauge = op.pack_gauge(u)
             psi = torch.randn(nrhs * V * 24, dtype=torch.float32, device="cuda", generator=gen)
@@ -310,7 +311,7 @@ def multi_rhs_variants(torch, steps, peak):
             ms = time_device(op, gauge, srcs, outs, max(10, steps // max(1, nrhs // 4)), 3, torch)
             sites = op.volume_cb * nrhs
             gbs = op.bytes_per_site * sites / (ms * 1e6)
-            out[f"{'f32' if fmt == 'native' else 'bf16'}_nrhs{nrhs}"] = {
+            out[f"{names[fmt]}_nrhs{nrhs}"] = {
                 "ms": ms, "gflops": 1320 * sites / (ms * 1e6), "gbs": gbs, "roofline_frac": gbs / peak,
                 "ms_per_rhs": ms / nrhs, "bytes_per_site_rhs": op.bytes_per_site, "variant": op.tuning()[1]}
             del gauge, srcs, outs

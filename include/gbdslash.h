@@ -90,10 +90,14 @@ int gbds_op_destroy(gbds_op op);
 #define GBDS_SPINOR_NATIVE 0   /* FP32 float4 or FP64 double2, as prec        */
 #define GBDS_SPINOR_BF16 1     /* 24 bfloat16 per spinor (48 B)                */
 #define GBDS_SPINOR_F16_NORM 2 /* 24 half scaled by a per-spinor float norm (52 B) */
+#define GBDS_SPINOR_F32_PAIRS 3 /* FP32 in spin pairs (96 B): 16-byte component c
+                                  * (0..2) = (s0c.r, s1c.r, s0c.i, s1c.i), 3 + c =
+                                  * (s2c.r, s3c.r, s2c.i, s3c.i); the operand
+                                  * layout of the fully packed kernel (variant 2) */
 
 /* As gbds_op_create, for nrhs right-hand sides per site (1..32; powers of two
- * have specialised kernels) and a spinor storage format.  nrhs > 1 or a 16-bit format needs
- * prec 32 and nd 4; arithmetic is FP32.  A field then holds nrhs spinors per
+ * have specialised kernels) and a spinor storage format.  nrhs > 1 or a format
+ * other than GBDS_SPINOR_NATIVE needs prec 32 and nd 4; arithmetic is FP32.  A field then holds nrhs spinors per
  * site, element (k, h, r) at k*stride*nrhs + h*nrhs + r (k: 16-byte component,
  * h: site, r: right-hand side), half formats followed by one float norm per
  * (h, r).  pack/unpack take FP32 packed arrays [nrhs][V][4][3][2]; the gauge
@@ -150,9 +154,10 @@ int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
  * uncapped; 1.. = variants that cap registers for more resident warps, which
  * launch 128-thread blocks.  Several rhs or 16-bit storage: 0 = the plain
  * multi-RHS kernel, 1 = the packed FP32x2 form (8, 16, 32 rhs; the block
- * size is fixed at 128), and for 16-bit storage 2 = projection, multiply and
- * reconstruction all in packed FP32x2 (8, 16, 32 rhs; 128-thread blocks).
- * Variants 1 and 2 run the plain kernel for other counts of rhs.
+ * size is fixed at 128), and for the 16-bit and FP32-pair formats 2 =
+ * projection, multiply and reconstruction all in packed FP32x2 (8, 16, 32
+ * rhs; 128-thread blocks).  Variants 1 and 2 run the plain kernel for other
+ * counts of rhs.
  * gbds_op_num_variants gives the count.  Used by the autotuner. */
 int gbds_op_set_tuning(gbds_op op, int threads, int variant);
 int gbds_op_get_tuning(gbds_op op, int *threads, int *variant);
@@ -164,9 +169,10 @@ int gbds_op_num_variants(gbds_op op);
  * for the same shape takes the cached choice without timing.  Operators with
  * several right-hand sides (or 16-bit storage) have these candidates: 0 the
  * plain multi-RHS kernel, 1 the colour multiply in packed FP32x2 arithmetic
- * on links staged per CTA (8, 16 or 32 rhs), for 16-bit formats 2 the whole
- * hop in packed FP32x2 (8, 16, 32 rhs) and with 16 or 32 rhs the
- * tensor-core kernel (gbds_op_set_tensor_cores).  Synchronises `stream`. */
+ * on links staged per CTA (8, 16 or 32 rhs), for the 16-bit and FP32-pair
+ * formats 2 the whole hop in packed FP32x2 (8, 16, 32 rhs) and, for 16-bit
+ * formats with 16 or 32 rhs, the tensor-core kernel
+ * (gbds_op_set_tensor_cores).  Synchronises `stream`. */
 int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream);
 
 /* Number of kernels this library has launched in this process (all kinds). */

@@ -99,10 +99,12 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     if (prec != 32 && prec != 64) return set_error(GBDS_ERROR_INVALID_VALUE, "prec must be 32 or 64");
     if (recon != 18 && recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "recon must be 18 or 12");
     if (nrhs < 1 || nrhs > 32) return set_error(GBDS_ERROR_INVALID_VALUE, "nrhs must be in [1, 32]");
-    if (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_BF16 && format != GBDS_SPINOR_F16_NORM)
+    if (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_BF16 && format != GBDS_SPINOR_F16_NORM &&
+        format != GBDS_SPINOR_F32_PAIRS)
         return set_error(GBDS_ERROR_INVALID_VALUE, "unknown spinor format");
     if ((nrhs > 1 || format != GBDS_SPINOR_NATIVE) && (prec != 32 || nd != 4))
-        return set_error(GBDS_ERROR_UNSUPPORTED, "several right-hand sides and 16-bit spinors need prec 32 and nd 4");
+        return set_error(GBDS_ERROR_UNSUPPORTED,
+                         "several right-hand sides and the non-native spinor formats need prec 32 and nd 4");
     Geom g;
     int rc = make_geom(dims, nd, &g);
     if (rc != GBDS_SUCCESS) return rc;
@@ -119,10 +121,10 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     o->nrhs = nrhs;
     o->format = format;
     // Single rhs: the register-cap variant (see above).  Several rhs or
-    // 16-bit storage: variant 0 = the plain multi-RHS kernel, 1 = its packed
-    // FP32x2 colour multiply, 2 = the whole hop packed (16-bit storage); from
-    // 16 rhs on (at 24^3x48) 2 is fastest for 16-bit storage and 1 for FP32
-    // (autotune chooses per shape).
+    // another format: variant 0 = the plain multi-RHS kernel, 1 = its packed
+    // FP32x2 colour multiply, 2 = the whole hop packed (16-bit and FP32-pair
+    // storage); from 16 rhs on (at 24^3x48) 2 is fastest where it exists and
+    // 1 for FP32 (autotune chooses per shape).
     const bool gen = nrhs > 1 || format != GBDS_SPINOR_NATIVE;
     const int gen_variant = nrhs >= 16 ? (format != GBDS_SPINOR_NATIVE ? 2 : 1) : 0;
     o->variant = gen ? gen_variant : ((prec == 32 && recon == 18) ? 1 : 0);
@@ -183,7 +185,8 @@ extern "C" int gbds_op_nrhs(gbds_op op) { return op ? op->nrhs : 0; }
 
 extern "C" int gbds_op_set_tensor_cores(gbds_op op, int on) {
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
-    if (on && (op->format == GBDS_SPINOR_NATIVE || (op->nrhs != 16 && op->nrhs != 32)))
+    if (on && ((op->format != GBDS_SPINOR_BF16 && op->format != GBDS_SPINOR_F16_NORM) ||
+               (op->nrhs != 16 && op->nrhs != 32)))
         return set_error(GBDS_ERROR_UNSUPPORTED, "tensor cores need a 16-bit spinor format and 16 or 32 right-hand sides");
     if (on && !op->d_err) {
         cudaError_t e = cudaMalloc(&op->d_err, sizeof(int));
@@ -244,7 +247,7 @@ extern "C" int gbds_op_set_tuning(gbds_op op, int threads, int variant) {
 
 extern "C" int gbds_op_num_variants(gbds_op op) {
     if (!op) return 0;
-    if (op->format != GBDS_SPINOR_NATIVE) return 3;  // + the fully packed 16-bit kernel
+    if (op->format != GBDS_SPINOR_NATIVE) return 3;  // variant 2: the fully packed kernel
     return op->nrhs > 1 ? 2 : dslash_variants(op->prec);
 }
 
@@ -255,7 +258,7 @@ std::map<std::array<int, 9>, std::array<int, 3>> g_tune_cache;
 }  // namespace
 
 static bool tc_eligible(gbds_op op) {
-    return op->format != GBDS_SPINOR_NATIVE && (op->nrhs == 16 || op->nrhs == 32);
+    return (op->format == GBDS_SPINOR_BF16 || op->format == GBDS_SPINOR_F16_NORM) && (op->nrhs == 16 || op->nrhs == 32);
 }
 
 extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream) {
@@ -353,9 +356,12 @@ extern "C" int gbds_op_pack_spinor(gbds_op op, const void *psi_packed, int parit
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (generic(op)) {
         const float *src = static_cast<const float *>(psi_packed);
-        cudaError_t e = op->format == GBDS_SPINOR_NATIVE
-                            ? launch_pack_gen_f32(op->g, op->nrhs, src, op->d_site_table, parity, spinor, st)
-                            : launch_pack_gen_half(op->format, op->g, op->nrhs, src, op->d_site_table, parity, spinor, st);
+        cudaError_t e =
+            op->format == GBDS_SPINOR_NATIVE
+                ? launch_pack_gen_f32(op->g, op->nrhs, src, op->d_site_table, parity, spinor, st)
+                : op->format == GBDS_SPINOR_F32_PAIRS
+                      ? launch_pack_gen_f32p(op->g, op->nrhs, src, op->d_site_table, parity, spinor, st)
+                      : launch_pack_gen_half(op->format, op->g, op->nrhs, src, op->d_site_table, parity, spinor, st);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_spinor");
     }
     cudaError_t e = launch_pack_spinor(op->g, op->prec, psi_packed, op->d_site_table, 0, parity, spinor, st);
@@ -370,9 +376,12 @@ extern "C" int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (generic(op)) {
         float *dst = static_cast<float *>(psi_packed);
-        cudaError_t e = op->format == GBDS_SPINOR_NATIVE
-                            ? launch_unpack_gen_f32(op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st)
-                            : launch_unpack_gen_half(op->format, op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st);
+        cudaError_t e =
+            op->format == GBDS_SPINOR_NATIVE
+                ? launch_unpack_gen_f32(op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st)
+                : op->format == GBDS_SPINOR_F32_PAIRS
+                      ? launch_unpack_gen_f32p(op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st)
+                      : launch_unpack_gen_half(op->format, op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "unpack_spinor");
     }
     cudaError_t e = launch_unpack_spinor(op->g, op->prec, spinor, op->d_site_table, 0, parity, psi_packed, st);
@@ -393,11 +402,15 @@ extern "C" int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, vo
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash (tensor cores)");
     }
     if (generic(op)) {
-        cudaError_t e = op->format == GBDS_SPINOR_NATIVE
-                            ? launch_gen_f32(op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f, nullptr, s,
-                                             op->variant)
-                            : launch_gen_half(op->format, op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr,
-                                              0.f, nullptr, s, op->variant);
+        cudaError_t e =
+            op->format == GBDS_SPINOR_NATIVE
+                ? launch_gen_f32(op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f, nullptr, s,
+                                 op->variant)
+                : op->format == GBDS_SPINOR_F32_PAIRS
+                      ? launch_gen_f32p(op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f, nullptr, s,
+                                        op->variant)
+                      : launch_gen_half(op->format, op->g, op->recon, op->nrhs, gauge, psi, res, isign, cb, nullptr, 0.f,
+                                        nullptr, s, op->variant);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
     }
     cudaError_t e = op->prec == 32 ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)

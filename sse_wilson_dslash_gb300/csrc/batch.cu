@@ -160,9 +160,11 @@ cudaError_t launch_batch(gbds_batch b, cudaStream_t st) {
     grid = std::max(1, std::min(grid, b->ntiles));
 #define GBDS_B(F, R) batch_kernel<F, R><<<grid, b->block, 0, st>>>(b->params, b->d_tiles, b->ntiles)
     if (b->recon == 18) {
-        if (b->format == 0) GBDS_B(kFmtNative, 18); else if (b->format == 1) GBDS_B(kFmtBF16, 18); else GBDS_B(kFmtF16N, 18);
+        if (b->format == 0) GBDS_B(kFmtNative, 18); else if (b->format == 1) GBDS_B(kFmtBF16, 18);
+        else if (b->format == 2) GBDS_B(kFmtF16N, 18); else GBDS_B(kFmtF32Pairs, 18);
     } else {
-        if (b->format == 0) GBDS_B(kFmtNative, 12); else if (b->format == 1) GBDS_B(kFmtBF16, 12); else GBDS_B(kFmtF16N, 12);
+        if (b->format == 0) GBDS_B(kFmtNative, 12); else if (b->format == 1) GBDS_B(kFmtBF16, 12);
+        else if (b->format == 2) GBDS_B(kFmtF16N, 12); else GBDS_B(kFmtF32Pairs, 12);
     }
 #undef GBDS_B
     count_launch();
@@ -176,7 +178,7 @@ extern "C" int gbds_batch_create(gbds_batch *out, const gbds_batch_item *items, 
     if (n > kMaxBatch) return set_error(GBDS_ERROR_INVALID_VALUE, "at most 32 lattices per batch");
     *out = nullptr;
     if (recon != 18 && recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "recon must be 18 or 12");
-    if (format < 0 || format > 2) return set_error(GBDS_ERROR_INVALID_VALUE, "unknown spinor format");
+    if (format < 0 || format > 3) return set_error(GBDS_ERROR_INVALID_VALUE, "unknown spinor format");
     gbds_batch b = new (std::nothrow) gbds_batch_s;
     if (!b) return set_error(GBDS_ERROR_OUT_OF_MEMORY, "host allocation failed");
     b->recon = recon;

@@ -10,7 +10,12 @@
 // 2 s + 2 nd g / NRHS (s, g = spinor, link bytes).
 //
 // Storage formats (SpinorIO):
-//   F32   6 float4 per spinor (96 B)
+//   F32   6 float4 per spinor (96 B): float4 k holds complex elements 2k and
+//         2k + 1 (element j = spin * 3 + colour), as the single-rhs kernel
+//   F32P  6 float4 per spinor (96 B) in spin pairs: float4 c (c = 0..2)
+//         holds (s0_c.r, s1_c.r, s0_c.i, s1_c.i), float4 3 + c holds
+//         (s2_c.r, s3_c.r, s2_c.i, s3_c.i) -- the operand pairs of the fully
+//         packed kernel
 //   BF16  3 uint4 per spinor, 24 bfloat16 (48 B)
 //   F16N  3 uint4 per spinor, 24 half scaled by a per-spinor float norm
 //         stored after the components (48 + 4 B): value = half * norm,
@@ -26,10 +31,33 @@
 
 namespace gbds {
 
-enum SpinorFormat { kFmtNative = 0, kFmtBF16 = 1, kFmtF16N = 2 };
+enum SpinorFormat { kFmtNative = 0, kFmtBF16 = 1, kFmtF16N = 2, kFmtF32Pairs = 3 };
 
 // Load/store of one spinor at element index i, component stride cs (elements).
 template <int FMT> struct Sio;
+
+template <>
+struct Sio<kFmtF32Pairs> {
+    static constexpr int kBytes = 96;
+    __device__ __forceinline__ static void load(const char *base, size_t cs, size_t i, cx<float> (&s)[4][3]) {
+        const float4 *p = reinterpret_cast<const float4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const float4 q = __ldg(p + k * cs + i);
+            const int a = k < 3 ? 0 : 2, c = k % 3;
+            s[a][c] = {q.x, q.z};
+            s[a + 1][c] = {q.y, q.w};
+        }
+    }
+    __device__ __forceinline__ static void store(char *base, size_t cs, size_t i, const cx<float> (&s)[4][3]) {
+        float4 *p = reinterpret_cast<float4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const int a = k < 3 ? 0 : 2, c = k % 3;
+            __stcs(p + k * cs + i, make_float4(s[a][c].r, s[a + 1][c].r, s[a][c].i, s[a + 1][c].i));
+        }
+    }
+};
 
 template <>
 struct Sio<kFmtNative> {
@@ -279,17 +307,18 @@ __device__ __forceinline__ void reconstruct_pairs(cx<float> (&acc)[4][3], const 
     }
 }
 
-// Variant 1's projection and reconstruction: in pairs for 16-bit storage
-// (measured faster), scalar for FP32 storage (measured slower in pairs).
+// Variant 1's projection and reconstruction: in (r, i) pairs for 16-bit
+// storage (measured faster), scalar for FP32 storage (measured slower in
+// pairs; the spin-pair layout has no (r, i) pairs in its registers).
 template <int FMT, int MU, int SIGMA>
 __device__ __forceinline__ void g2_project(const cx<float> (&s)[4][3], cx<float> (&h)[2][3]) {
-    if constexpr (FMT == kFmtNative) project<MU, SIGMA>(s, h);
+    if constexpr (FMT == kFmtNative || FMT == kFmtF32Pairs) project<MU, SIGMA>(s, h);
     else project_pairs<MU, SIGMA>(s, h);
 }
 
 template <int FMT, int MU, int SIGMA>
 __device__ __forceinline__ void g2_reconstruct(cx<float> (&acc)[4][3], const cx<float> (&w)[2][3]) {
-    if constexpr (FMT == kFmtNative) reconstruct<MU, SIGMA>(acc, w);
+    if constexpr (FMT == kFmtNative || FMT == kFmtF32Pairs) reconstruct<MU, SIGMA>(acc, w);
     else reconstruct_pairs<MU, SIGMA>(acc, w);
 }
 
@@ -396,12 +425,14 @@ __global__ void __launch_bounds__(128, 6) dslash_gen2_kernel(const GenArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Fully packed variant for 16-bit spinors (BF16, half + norm), NRHS 8..32:
-// projection, colour multiply and reconstruction all run on pairs holding
-// the same part (real or imaginary) of the two spin halves,
+// Fully packed variant (NRHS 8..32): projection, colour multiply and
+// reconstruction all run on pairs holding the same part (real or imaginary)
+// of the two spin halves,
 //   R_c = (h0_c.r, h1_c.r),  I_c = (h0_c.i, h1_c.i),
-// one __ffma2_rn / __fadd2_rn per two reals and no operand moves: the
-// 16-bit -> FP32 conversion writes each value straight into its pair.
+// one __ffma2_rn / __fadd2_rn per two reals.  The 16-bit -> FP32 conversion
+// writes each value straight into its pair; FP32 storage is laid out in
+// these pairs in its F32P format (only mu = 0, 1, whose projection pairs
+// spin 0 with 3 and 1 with 2, take moves).
 //   projection  R_c = (s0_c.r, s1_c.r) + (g0, g1) * (part of s_j0_c, s_j1_c)
 //   multiply    W_R = sum_j Mr R_j - Mi I_j,   W_I = sum_j Mr I_j + Mi R_j
 //   upper       (acc0, acc1) += W
@@ -420,30 +451,45 @@ struct CPart {
     static constexpr float sim = (CODE == 0 || CODE == 2) ? 1.f : -1.f;
 };
 
-// the 24 reals of a stored 16-bit spinor, (s[j/3][j%3].r, .i) at 2j, 2j+1;
-// returns the scale (the norm of half + norm, 1 for BF16)
+// the 24 reals of a stored spinor, (s[j/3][j%3].r, .i) at 2j, 2j+1; returns
+// the scale (the norm of half + norm, else 1)
 template <int FMT>
-__device__ __forceinline__ float load_reals16(const char *base, size_t cs, size_t i, float (&v)[24]) {
-    static_assert(FMT == kFmtBF16 || FMT == kFmtF16N, "16-bit formats");
-    const uint4 *p = reinterpret_cast<const uint4 *>(base);
+__device__ __forceinline__ float load_reals(const char *base, size_t cs, size_t i, float (&v)[24]) {
+    static_assert(FMT == kFmtF32Pairs || FMT == kFmtBF16 || FMT == kFmtF16N, "pair-friendly formats");
+    if constexpr (FMT == kFmtF32Pairs) {
+        // the pair layout: no moves for the projection's operand pairs
+        const float4 *p = reinterpret_cast<const float4 *>(base);
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const uint4 q = __ldg(p + k * cs + i);
-        const unsigned w[4] = {q.x, q.y, q.z, q.w};
+        for (int k = 0; k < 6; k++) {
+            const float4 q = __ldg(p + k * cs + i);
+            const int a = k < 3 ? 0 : 2, c = k % 3;
+            v[2 * (3 * a + c)] = q.x;
+            v[2 * (3 * a + c) + 1] = q.z;
+            v[2 * (3 * a + 3 + c)] = q.y;
+            v[2 * (3 * a + 3 + c) + 1] = q.w;
+        }
+        return 1.f;
+    } else {
+        const uint4 *p = reinterpret_cast<const uint4 *>(base);
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            if constexpr (FMT == kFmtBF16) {
-                v[8 * k + 2 * c] = __uint_as_float(w[c] << 16);
-                v[8 * k + 2 * c + 1] = __uint_as_float(w[c] & 0xffff0000u);
-            } else {
-                const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[c]));
-                v[8 * k + 2 * c] = f.x;
-                v[8 * k + 2 * c + 1] = f.y;
+        for (int k = 0; k < 3; k++) {
+            const uint4 q = __ldg(p + k * cs + i);
+            const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                if constexpr (FMT == kFmtBF16) {
+                    v[8 * k + 2 * c] = __uint_as_float(w[c] << 16);
+                    v[8 * k + 2 * c + 1] = __uint_as_float(w[c] & 0xffff0000u);
+                } else {
+                    const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[c]));
+                    v[8 * k + 2 * c] = f.x;
+                    v[8 * k + 2 * c + 1] = f.y;
+                }
             }
         }
+        if constexpr (FMT == kFmtF16N) return __ldg(Sio<kFmtF16N>::norms(base, cs) + i);
+        else return 1.f;
     }
-    if constexpr (FMT == kFmtF16N) return __ldg(Sio<kFmtF16N>::norms(base, cs) + i);
-    else return 1.f;
 }
 
 // One hop: project v (scaled by nrm for half + norm), multiply by the staged
@@ -495,7 +541,7 @@ __device__ __forceinline__ void packed_hop(const float (&v)[24], float nrm, cons
     }
 }
 
-template <int FMT, int RECON, int ISIGN, int NRHS>
+template <int FMT, int RECON, int ISIGN, int NRHS, int EPI>
 __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
     static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
     constexpr int P = 128 / NRHS;  // sites per CTA
@@ -527,6 +573,7 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
             }
     }
     __syncthreads();
+    float nrm = 0.f;
     if (act) {
         float2 UR[3], UI[3], LR[3], LI[3];
 #pragma unroll
@@ -534,9 +581,9 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
 #define GBDS_G3_HOP(MU, LORD)                                                                            \
     {                                                                                                    \
         float v[24];                                                                                     \
-        float sc = load_reals16<FMT>(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, v);                        \
+        float sc = load_reals<FMT>(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, v);                        \
         packed_hop<MU, ISIGN, LORD, SCALE>(v, sc, sL[p][2 * MU], UR, UI, LR, LI);                        \
-        sc = load_reals16<FMT>(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, v);                              \
+        sc = load_reals<FMT>(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, v);                              \
         packed_hop<MU, -ISIGN, LORD, SCALE>(v, sc, sL[p][2 * MU + 1], UR, UI, LR, LI);                   \
     }
         GBDS_G3_HOP(0, 1)
@@ -557,7 +604,24 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
             acc[2][c] = {LR[c].x, LI[c].x};
             acc[3][c] = {LR[c].y, LI[c].y};
         }
-        Sio<FMT>::store(a.res, a.cs, (size_t)h * NRHS + r, acc);
+        const size_t i = (size_t)h * NRHS + r;
+        if constexpr (EPI) {
+            cx<float> xv[4][3];
+            Sio<FMT>::load(a.x, a.cs, i, xv);
+#pragma unroll
+            for (int s = 0; s < 4; s++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    acc[s][c].r = fmaf(a.coef, acc[s][c].r, xv[s][c].r);
+                    acc[s][c].i = fmaf(a.coef, acc[s][c].i, xv[s][c].i);
+                    nrm = fmaf(acc[s][c].r, acc[s][c].r, nrm);
+                    nrm = fmaf(acc[s][c].i, acc[s][c].i, nrm);
+                }
+        }
+        Sio<FMT>::store(a.res, a.cs, i, acc);
+    }
+    if constexpr (EPI == 2) {
+        if (a.partials) block_sum_rhs<NRHS>(a.partials, nrm);
     }
 }
 

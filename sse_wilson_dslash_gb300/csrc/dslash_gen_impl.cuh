@@ -96,13 +96,13 @@ void launch_gen2_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
     }
 }
 
-template <int FMT, int RECON, int ISIGN>
+template <int FMT, int RECON, int ISIGN, int EPI>
 void launch_gen3_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
     const unsigned vh = (unsigned)a.g.Vh;
     switch (nrhs) {
-    case 8: dslash_gen3_kernel<FMT, RECON, ISIGN, 8><<<(vh + 15) / 16, 128, 0, st>>>(a); break;
-    case 16: dslash_gen3_kernel<FMT, RECON, ISIGN, 16><<<(vh + 7) / 8, 128, 0, st>>>(a); break;
-    default: dslash_gen3_kernel<FMT, RECON, ISIGN, 32><<<(vh + 3) / 4, 128, 0, st>>>(a); break;
+    case 8: dslash_gen3_kernel<FMT, RECON, ISIGN, 8, EPI><<<(vh + 15) / 16, 128, 0, st>>>(a); break;
+    case 16: dslash_gen3_kernel<FMT, RECON, ISIGN, 16, EPI><<<(vh + 7) / 8, 128, 0, st>>>(a); break;
+    default: dslash_gen3_kernel<FMT, RECON, ISIGN, 32, EPI><<<(vh + 3) / 4, 128, 0, st>>>(a); break;
     }
 }
 
@@ -128,14 +128,20 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     if (epi && (nrhs > 32 || (nrhs & (nrhs - 1)) != 0)) return cudaErrorInvalidValue;
     const bool packed_nrhs = nrhs == 8 || nrhs == 16 || nrhs == 32;
     const bool v2 = variant == 1 && packed_nrhs;
-    // variant 2 (fully packed, no epilogue) exists for the 16-bit formats;
-    // like variant 1, it falls back to the plain kernel otherwise
-    const bool v3 = variant == 2 && packed_nrhs && FMT != kFmtNative && !epi;
+    // variant 2 (fully packed: 16-bit and FP32-pair storage; its xpay
+    // epilogue serves the batched solver's FP32-pair fields); like variant 1,
+    // it falls back to the plain kernel otherwise
+    const bool v3 = variant == 2 && packed_nrhs && FMT != kFmtNative && (FMT == kFmtF32Pairs || !epi);
 #define GBDS_GEN(R, S)                                                   \
     do {                                                                 \
         if constexpr (FMT != kFmtNative) {                               \
             if (v3) {                                                    \
-                launch_gen3_nrhs<FMT, R, S>(a, nrhs, st);                \
+                if constexpr (FMT == kFmtF32Pairs) {                     \
+                    if (epi) launch_gen3_nrhs<FMT, R, S, 2>(a, nrhs, st); \
+                    else launch_gen3_nrhs<FMT, R, S, 0>(a, nrhs, st);    \
+                } else {                                                 \
+                    launch_gen3_nrhs<FMT, R, S, 0>(a, nrhs, st);         \
+                }                                                        \
                 break;                                                   \
             }                                                            \
         }                                                                \

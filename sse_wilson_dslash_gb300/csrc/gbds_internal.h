@@ -53,13 +53,17 @@ cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_
                               const int *site_table, void *gauge, cudaStream_t stream);
 
 // Generalised Dslash (dslash_gen_*.cu): FP32 arithmetic and links, nrhs in
-// {1,2,4,8,16,32}, spinor formats 0 FP32, 1 BF16, 2 FP16 + norm.  x != nullptr
-// selects the xpay epilogue res = x + coef * D psi (nrhs 1 only) with |res|^2
-// partials per 128-thread block.
+// {1,2,4,8,16,32}, spinor formats 0 FP32, 1 BF16, 2 FP16 + norm, 3 FP32 in
+// spin pairs.  x != nullptr selects the xpay epilogue res = x + coef * D psi
+// with |res|^2 partials (one per 128-thread block for nrhs 1, one per block
+// and rhs otherwise).
 // variant 1: the colour multiply in packed FP32x2 arithmetic on links staged
-// per CTA (nrhs 8, 16, 32; other counts take variant 0).
+// per CTA (nrhs 8, 16, 32; other counts take variant 0).  variant 2 (formats
+// 1, 2, 3): the whole hop in packed FP32x2 (nrhs 8, 16, 32).
 cudaError_t launch_gen_f32(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
                            int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0);
+cudaError_t launch_gen_f32p(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
+                            int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0);
 cudaError_t launch_gen_half(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,
                             int isign, int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0);
 // packed: FP32 [nrhs][V][4][3][2], caller order
@@ -67,11 +71,15 @@ cudaError_t launch_pack_gen_f32(const Geom &g, int nrhs, const float *packed, co
                                 cudaStream_t st);
 cudaError_t launch_unpack_gen_f32(const Geom &g, int nrhs, const void *in, const int *table, int parity, float *packed,
                                   cudaStream_t st);
+cudaError_t launch_pack_gen_f32p(const Geom &g, int nrhs, const float *packed, const int *table, int parity, void *out,
+                                 cudaStream_t st);
+cudaError_t launch_unpack_gen_f32p(const Geom &g, int nrhs, const void *in, const int *table, int parity, float *packed,
+                                   cudaStream_t st);
 cudaError_t launch_pack_gen_half(int fmt, const Geom &g, int nrhs, const float *packed, const int *table, int parity,
                                  void *out, cudaStream_t st);
 cudaError_t launch_unpack_gen_half(int fmt, const Geom &g, int nrhs, const void *in, const int *table, int parity,
                                    float *packed, cudaStream_t st);
-inline int gen_spinor_bytes(int fmt) { return fmt == 0 ? 96 : (fmt == 1 ? 48 : 52); }
+inline int gen_spinor_bytes(int fmt) { return (fmt == 0 || fmt == 3) ? 96 : (fmt == 1 ? 48 : 52); }
 // Tensor-core form (dslash_tc.cu): fmt 1 / 2, nrhs 16 or 32, FP32 links
 // converted to the 16-bit operand type; err set to 1 on a timed-out wait.
 cudaError_t launch_gen_tc(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,

@@ -1028,10 +1028,14 @@ __global__ void __launch_bounds__(128) bdemote(const double2 *__restrict__ r64, 
                                               int Vh, int stride, int nrhs, int q, size_t cs) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= Vh) return;
+    // the inner fields are FP32 spin pairs: float4 k holds complex elements
+    // e0 and e0 + 3 (spins 0/1 or 2/3 of colour k % 3) as (e0.r, e1.r, e0.i,
+    // e1.i)
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        const double2 a = r64[(size_t)(2 * k) * stride + h], b = r64[(size_t)(2 * k + 1) * stride + h];
-        const float4 f = make_float4((float)(a.x * inv), (float)(a.y * inv), (float)(b.x * inv), (float)(b.y * inv));
+        const int e0 = (k < 3 ? 0 : 6) + k % 3;
+        const double2 a = r64[(size_t)e0 * stride + h], b = r64[(size_t)(e0 + 3) * stride + h];
+        const float4 f = make_float4((float)(a.x * inv), (float)(b.x * inv), (float)(a.y * inv), (float)(b.y * inv));
         const size_t i = (size_t)k * cs + (size_t)h * nrhs + q;
         r[i] = f;
         p[i] = f;
@@ -1045,12 +1049,13 @@ __global__ void __launch_bounds__(128) bpromote(const float4 *__restrict__ e, do
     if (h >= Vh) return;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
+        const int e0 = (k < 3 ? 0 : 6) + k % 3;  // the pair layout, as in bdemote
         const float4 v = e[(size_t)k * cs + (size_t)h * nrhs + q];
-        double2 &a = x64[(size_t)(2 * k) * stride + h];
-        double2 &b = x64[(size_t)(2 * k + 1) * stride + h];
+        double2 &a = x64[(size_t)e0 * stride + h];
+        double2 &b = x64[(size_t)(e0 + 3) * stride + h];
         a.x = fma(s, (double)v.x, a.x);
-        a.y = fma(s, (double)v.y, a.y);
-        b.x = fma(s, (double)v.z, b.x);
+        a.y = fma(s, (double)v.z, a.y);
+        b.x = fma(s, (double)v.y, b.x);
         b.y = fma(s, (double)v.w, b.y);
     }
 }
@@ -1095,12 +1100,13 @@ cudaError_t bfinish_on(gbds_bsolver b, int mode, cudaStream_t st) {
 cudaError_t apply_Mb(gbds_bsolver b, const void *in, void *out, int isign, double *partials, cudaStream_t st) {
     gbds_solver s = b->s1;
     const float k2 = (float)(s->prm.kappa * s->prm.kappa);
-    // the packed FP32x2 kernel from 16 rhs on (measured faster there)
-    const int v = b->nrhs >= 16 ? 1 : 0;
+    // inner fields in FP32 spin pairs: the fully packed FP32x2 kernel from 16
+    // rhs on (measured faster there)
+    const int v = b->nrhs >= 16 ? 2 : 0;
     cudaError_t e =
-        launch_gen_f32(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, isign, 0, nullptr, 0.f, nullptr, st, v);
+        launch_gen_f32p(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, isign, 0, nullptr, 0.f, nullptr, st, v);
     if (e != cudaSuccess) return e;
-    return launch_gen_f32(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, out, isign, 1, in, -k2, partials, st, v);
+    return launch_gen_f32p(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, out, isign, 1, in, -k2, partials, st, v);
 }
 
 cudaError_t read_bscalars(gbds_bsolver b, cudaStream_t st) {

@@ -77,6 +77,28 @@ def test_op_create_validation(libs):
             assert L.gbds_get_last_error()
 
 
+def test_spinor_formats_and_their_variants(libs):
+    """Formats 0..3 (FP32, BF16, half + norm, FP32 spin pairs) with several
+    right-hand sides: field sizes, kernel variants, tensor-core eligibility
+    (16-bit formats only); no device work."""
+    from sse_wilson_dslash_gb300 import _lib
+    L = _lib.core()
+    h = ctypes.c_void_p()
+    d = (ctypes.c_int * 4)(4, 4, 4, 4)
+    for fmt, nbytes, nv in ((0, 96, 2), (1, 48, 3), (2, 52, 3), (3, 96, 3)):
+        assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 32, 18, 32, fmt) == 0, L.gbds_get_last_error()
+        V, Vh, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        assert L.gbds_op_geometry(h, ctypes.byref(V), ctypes.byref(Vh), ctypes.byref(st)) == 0
+        assert L.gbds_op_spinor_bytes(h) == nbytes * st.value * 32
+        assert L.gbds_op_num_variants(h) == nv
+        if fmt in (0, 3):
+            assert L.gbds_op_set_tensor_cores(h, 1) != 0
+        L.gbds_op_destroy(h)
+    assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 32, 18, 4, 4) != 0
+    # the non-native formats need prec 32 and nd 4
+    assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 64, 18, 1, 3) != 0
+
+
 def test_set_layout_rejects_non_permutations(libs):
     from sse_wilson_dslash_gb300 import _lib
     L = _lib.core()

@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 # Per-site tolerances: FP32 as the parity tests; bfloat16 storage rounds
 # inputs and outputs to 8 significant bits (2^-9 relative per component);
 # half + norm to 11 bits of the site's largest component.
-TOL = {"native": 1e-6, "bf16": 1.2e-2, "f16": 3e-3}
+TOL = {"native": 1e-6, "f32_pairs": 1e-6, "bf16": 1.2e-2, "f16": 3e-3}
 
 
 def _round(psi, fmt):
@@ -26,7 +26,7 @@ def _round(psi, fmt):
     return psi.astype(np.float32).astype(np.float64)
 
 
-@pytest.mark.parametrize("fmt", ["native", "bf16", "f16"])
+@pytest.mark.parametrize("fmt", ["native", "f32_pairs", "bf16", "f16"])
 @pytest.mark.parametrize("nrhs", [1, 2, 4, 8, 16, 32])
 def test_multi_rhs_matches_oracle(nrhs, fmt):
     import torch
@@ -105,7 +105,7 @@ def test_tensor_core_multi_rhs_matches_oracle(nrhs, fmt, dims):
 def test_tensor_cores_need_16bit_and_16_or_32_rhs():
     from sse_wilson_dslash_gb300.device import DslashOperator
     from sse_wilson_dslash_gb300 import _lib
-    for nrhs, fmt in ((32, "native"), (8, "bf16"), (1, "f16")):
+    for nrhs, fmt in ((32, "native"), (32, "f32_pairs"), (8, "bf16"), (1, "f16")):
         op = DslashOperator((4, 4, 4, 4), nrhs=nrhs, spinor_format=fmt)
         with pytest.raises(_lib.GbdsError):
             op.set_tensor_cores(True)
@@ -217,12 +217,12 @@ def test_tensor_core_production_lattice():
         assert O.site_rel_err(got, ref, O.target_sites(4, dims, lol, 0)) <= TOL[fmt], r
 
 
-@pytest.mark.parametrize("fmt", ["native", "bf16", "f16"])
+@pytest.mark.parametrize("fmt", ["native", "f32_pairs", "bf16", "f16"])
 @pytest.mark.parametrize("nrhs", [8, 16, 32])
 def test_packed_fp32x2_variant_matches_oracle(nrhs, fmt):
-    """Variant 1 of the multi-RHS kernel (links staged per CTA, colour
-    multiply in packed FP32x2 arithmetic) and, for 16-bit storage, variant 2
-    (the whole hop in packed FP32x2) against the oracle."""
+    """Variants 1 (links staged per CTA, colour multiply in packed FP32x2
+    arithmetic) and 2 (the whole hop in packed FP32x2; 16-bit and FP32-pair
+    storage) of the multi-RHS kernel against the oracle."""
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
     dims = (8, 4, 6, 4)
