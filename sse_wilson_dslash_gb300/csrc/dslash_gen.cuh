@@ -351,6 +351,8 @@ __device__ __forceinline__ void su3_mul_splat(const float4 *M, const cx<float> (
 template <int FMT, int RECON, int ISIGN, int NRHS, int EPI>
 __global__ void __launch_bounds__(128, 6) dslash_gen2_kernel(const GenArgs a) {
     static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
+    pdl_allow_next();
+    pdl_wait_prev();
     constexpr int P = 128 / NRHS;  // sites per CTA
     __shared__ float4 sL[P][8][9];
     const int t = threadIdx.x;
@@ -544,6 +546,8 @@ __device__ __forceinline__ void packed_hop(const float (&v)[24], float nrm, cons
 template <int FMT, int RECON, int ISIGN, int NRHS, int EPI>
 __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
     static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
+    pdl_allow_next();
+    pdl_wait_prev();
     constexpr int P = 128 / NRHS;  // sites per CTA
     constexpr bool SCALE = FMT == kFmtF16N;
     __shared__ float4 sL[P][8][9];
@@ -630,6 +634,8 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
 // same with one partial per block and rhs (NRHS 2..32, 128-thread blocks).
 template <int FMT, int RECON, int ISIGN, int NRHS, int EPI, int LFMT = 0>
 __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nr = nrhs_of<NRHS>(a);
     const int h = t / nr, r = t - h * nr;

@@ -46,13 +46,13 @@ template <int FMT, int RECON, int ISIGN, int EPI>
 void launch_gen_nrhs(const GenArgs &a, int nrhs, dim3 grid, cudaStream_t st) {
     constexpr int E1 = EPI == 1 ? 1 : 0;  // nrhs 1 takes the single-sum epilogue
     switch (nrhs) {
-    case 1: if constexpr (EPI != 2) dslash_gen_kernel<FMT, RECON, ISIGN, 1, E1><<<grid, 128, 0, st>>>(a); break;
-    case 2: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 2, EPI><<<grid, 128, 0, st>>>(a); break;
-    case 4: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 4, EPI><<<grid, 128, 0, st>>>(a); break;
-    case 8: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 8, EPI><<<grid, 128, 0, st>>>(a); break;
-    case 16: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 16, EPI><<<grid, 128, 0, st>>>(a); break;
-    case 32: if constexpr (EPI != 1) dslash_gen_kernel<FMT, RECON, ISIGN, 32, EPI><<<grid, 128, 0, st>>>(a); break;
-    default: if constexpr (EPI == 0) dslash_gen_kernel<FMT, RECON, ISIGN, 0, 0><<<grid, 128, 0, st>>>(a); break;
+    case 1: if constexpr (EPI != 2) launch_pdl(dslash_gen_kernel<FMT, RECON, ISIGN, 1, E1>, grid, 128, st, a); break;
+    case 2: if constexpr (EPI != 1) launch_pdl(dslash_gen_kernel<FMT, RECON, ISIGN, 2, EPI>, grid, 128, st, a); break;
+    case 4: if constexpr (EPI != 1) launch_pdl(dslash_gen_kernel<FMT, RECON, ISIGN, 4, EPI>, grid, 128, st, a); break;
+    case 8: if constexpr (EPI != 1) launch_pdl(dslash_gen_kernel<FMT, RECON, ISIGN, 8, EPI>, grid, 128, st, a); break;
+    case 16: if constexpr (EPI != 1) launch_pdl(dslash_gen_kernel<FMT, RECON, ISIGN, 16, EPI>, grid, 128, st, a); break;
+    case 32: if constexpr (EPI != 1) launch_pdl(dslash_gen_kernel<FMT, RECON, ISIGN, 32, EPI>, grid, 128, st, a); break;
+    default: if constexpr (EPI == 0) launch_pdl(dslash_gen_kernel<FMT, RECON, ISIGN, 0, 0>, grid, 128, st, a); break;
     }
 }
 
@@ -73,7 +73,7 @@ cudaError_t launch_gen_h16_t(const Geom &g, int recon, const void *gauge, const 
     a.coef = coef;
     a.partials = partials;
     const dim3 grid((unsigned)((g.Vh + 127) / 128));
-#define GBDS_H(R, S, E) dslash_gen_kernel<FMT, R, S, 1, E, 1><<<grid, 128, 0, st>>>(a)
+#define GBDS_H(R, S, E) launch_pdl(dslash_gen_kernel<FMT, R, S, 1, E, 1>, grid, 128, st, a)
     if (x) {
         if (recon == 18) { if (isign > 0) GBDS_H(18, 1, 1); else GBDS_H(18, -1, 1); }
         else             { if (isign > 0) GBDS_H(12, 1, 1); else GBDS_H(12, -1, 1); }
@@ -90,9 +90,9 @@ template <int FMT, int RECON, int ISIGN, int EPI>
 void launch_gen2_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
     const unsigned vh = (unsigned)a.g.Vh;
     switch (nrhs) {
-    case 8: dslash_gen2_kernel<FMT, RECON, ISIGN, 8, EPI><<<(vh + 15) / 16, 128, 0, st>>>(a); break;
-    case 16: dslash_gen2_kernel<FMT, RECON, ISIGN, 16, EPI><<<(vh + 7) / 8, 128, 0, st>>>(a); break;
-    default: dslash_gen2_kernel<FMT, RECON, ISIGN, 32, EPI><<<(vh + 3) / 4, 128, 0, st>>>(a); break;
+    case 8: launch_pdl(dslash_gen2_kernel<FMT, RECON, ISIGN, 8, EPI>, dim3((vh + 15) / 16), 128, st, a); break;
+    case 16: launch_pdl(dslash_gen2_kernel<FMT, RECON, ISIGN, 16, EPI>, dim3((vh + 7) / 8), 128, st, a); break;
+    default: launch_pdl(dslash_gen2_kernel<FMT, RECON, ISIGN, 32, EPI>, dim3((vh + 3) / 4), 128, st, a); break;
     }
 }
 
@@ -100,9 +100,9 @@ template <int FMT, int RECON, int ISIGN, int EPI>
 void launch_gen3_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
     const unsigned vh = (unsigned)a.g.Vh;
     switch (nrhs) {
-    case 8: dslash_gen3_kernel<FMT, RECON, ISIGN, 8, EPI><<<(vh + 15) / 16, 128, 0, st>>>(a); break;
-    case 16: dslash_gen3_kernel<FMT, RECON, ISIGN, 16, EPI><<<(vh + 7) / 8, 128, 0, st>>>(a); break;
-    default: dslash_gen3_kernel<FMT, RECON, ISIGN, 32, EPI><<<(vh + 3) / 4, 128, 0, st>>>(a); break;
+    case 8: launch_pdl(dslash_gen3_kernel<FMT, RECON, ISIGN, 8, EPI>, dim3((vh + 15) / 16), 128, st, a); break;
+    case 16: launch_pdl(dslash_gen3_kernel<FMT, RECON, ISIGN, 16, EPI>, dim3((vh + 7) / 8), 128, st, a); break;
+    default: launch_pdl(dslash_gen3_kernel<FMT, RECON, ISIGN, 32, EPI>, dim3((vh + 3) / 4), 128, st, a); break;
     }
 }
 

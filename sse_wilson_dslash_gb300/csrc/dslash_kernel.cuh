@@ -324,12 +324,22 @@ __device__ __forceinline__ void hop_pair(const DslashArgs<T> &a, int h, const Nb
 template <int MINB> struct Bounds { static constexpr int threads = 128, blocks = MINB; };
 template <> struct Bounds<0> { static constexpr int threads = 256, blocks = 1; };
 
+// Programmatic dependent launch: the next kernel launched on the stream with
+// the programmatic-serialisation attribute may start its blocks once every
+// block of this grid has started; it waits (griddepcontrol.wait) for this
+// grid's completion and memory before its first global read.  Without the
+// attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait_prev() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <typename T, int ND, int RECON, int ISIGN, int MINB>
 __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks) dslash_kernel(const DslashArgs<T> a) {
+    pdl_allow_next();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= a.g.Vh) return;
     Nbr n;
-    neighbours<ND>(a.g, h, a.pt, n);
+    if (h < a.g.Vh) neighbours<ND>(a.g, h, a.pt, n);  // index arithmetic only: overlaps the previous grid
+    pdl_wait_prev();
+    if (h >= a.g.Vh) return;
     cx<T> acc[4][3];
 #pragma unroll
     for (int s = 0; s < 4; s++)
@@ -347,9 +357,25 @@ template <typename T> struct Variants;
 template <> struct Variants<float> { static constexpr int n = 5; static constexpr int minb[5] = {0, 6, 7, 8, 10}; };
 template <> struct Variants<double> { static constexpr int n = 3; static constexpr int minb[3] = {0, 3, 4}; };
 
+// Launch with the programmatic-serialisation attribute (see pdl_wait_prev).
+template <typename... P, typename... A>
+void launch_pdl(void (*kernel)(P...), dim3 grid, int block, cudaStream_t stream, const A &...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <typename T, int MINB>
 void launch_variant(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, cudaStream_t stream) {
-#define GBDS_LAUNCH(ND, R, S) dslash_kernel<T, ND, R, S, MINB><<<grid, block, 0, stream>>>(a)
+#define GBDS_LAUNCH(ND, R, S) launch_pdl(dslash_kernel<T, ND, R, S, MINB>, grid, block, stream, a)
     if (nd == 4) {
         if (recon == 18) { if (isign > 0) GBDS_LAUNCH(4, 18, 1); else GBDS_LAUNCH(4, 18, -1); }
         else             { if (isign > 0) GBDS_LAUNCH(4, 12, 1); else GBDS_LAUNCH(4, 12, -1); }
@@ -392,6 +418,8 @@ __device__ __forceinline__ void block_sum_to(double *partials, T v) {
 template <typename T, int RECON, int ISIGN, int MINB>
 __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks)
     dslash_xpay_kernel(const DslashArgs<T> a, const typename VecOf<T>::S *__restrict__ x, T coef, double *partials) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     T nrm = 0;
     if (h < a.g.Vh) {
@@ -444,11 +472,11 @@ cudaError_t launch_dslash_xpay_t(const Geom &g, int recon, const void *gauge, co
     const auto *xv = static_cast<const typename VecOf<T>::S *>(x);
     constexpr int m18 = XpayMinb<T>::r18, m12 = XpayMinb<T>::r12;
     if (recon == 18) {
-        if (isign > 0) dslash_xpay_kernel<T, 18, 1, m18><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
-        else dslash_xpay_kernel<T, 18, -1, m18><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
+        if (isign > 0) launch_pdl(dslash_xpay_kernel<T, 18, 1, m18>, grid, 128, stream, a, xv, coef, partials);
+        else launch_pdl(dslash_xpay_kernel<T, 18, -1, m18>, grid, 128, stream, a, xv, coef, partials);
     } else {
-        if (isign > 0) dslash_xpay_kernel<T, 12, 1, m12><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
-        else dslash_xpay_kernel<T, 12, -1, m12><<<grid, 128, 0, stream>>>(a, xv, coef, partials);
+        if (isign > 0) launch_pdl(dslash_xpay_kernel<T, 12, 1, m12>, grid, 128, stream, a, xv, coef, partials);
+        else launch_pdl(dslash_xpay_kernel<T, 12, -1, m12>, grid, 128, stream, a, xv, coef, partials);
     }
     count_launch();
     return cudaGetLastError();
