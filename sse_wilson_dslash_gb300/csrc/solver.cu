@@ -64,6 +64,8 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) cg_update(SV<T> *x, SV<T> *r, const SV<T> *__restrict__ p,
                                                      const SV<T> *__restrict__ Ap, const Scalars *sc, int Vh, int stride,
                                                      double *partials) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     T nrm = 0;
     if (h < Vh) {
@@ -84,6 +86,8 @@ __global__ void __launch_bounds__(kThreads) cg_update(SV<T> *x, SV<T> *r, const 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) cg_xpay(const SV<T> *__restrict__ r, SV<T> *p, const Scalars *sc, int Vh,
                                                    int stride) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= Vh) return;
     const T b = (T)sc->beta;
@@ -228,6 +232,8 @@ __device__ __forceinline__ float4 pair(const cx<float> (&s)[4][3], int k) {
 template <int FMT>
 __global__ void __launch_bounds__(kThreads) cg_update_h(float4 *x, float4 *r, const char *p, const char *Ap,
                                                        const Scalars *sc, int Vh, int stride, double *partials) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     float nrm = 0.f;
     if (h < Vh) {
@@ -251,6 +257,8 @@ __global__ void __launch_bounds__(kThreads) cg_update_h(float4 *x, float4 *r, co
 template <int FMT>
 __global__ void __launch_bounds__(kThreads) cg_xpay_h(const float4 *__restrict__ r, char *p, const Scalars *sc, int Vh,
                                                      int stride) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= Vh) return;
     const float b = (float)sc->beta;
@@ -308,6 +316,8 @@ enum FinishMode { kAlpha = 0, kBeta = 1, kSetRR = 2, kOuterRR = 3, kNorm = 4 };
 
 // Deterministic sum of the block partials (fixed order), then the scalar step.
 __global__ void __launch_bounds__(1024) finish(const double *partials, int n, Scalars *sc, int mode) {
+    pdl_allow_next();
+    pdl_wait_prev();
     __shared__ double buf[1024];
     double t = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) t += partials[i];
@@ -376,7 +386,7 @@ cudaError_t dslash_xpay(const Geom &g, int recon, const void *gauge, const void 
 }
 
 cudaError_t finish_on(gbds_solver s, int mode, cudaStream_t st) {
-    finish<<<1, 1024, 0, st>>>(s->partials, blocks(s->g), s->sc, mode);
+    launch_pdl(finish, dim3(1), 1024, st, s->partials, blocks(s->g), s->sc, mode);
     count_launch();
     return cudaGetLastError();
 }
@@ -429,16 +439,16 @@ cudaError_t cg(gbds_solver s, const void *gauge, int recon, void *x, void *r, vo
         if (e == cudaSuccess) e = finish_on(s, kAlpha, st);
         if (e == cudaSuccess) e = apply_M<T>(s, gauge, recon, Mp, t, Ap, -1, nullptr, st);
         if (e == cudaSuccess) {
-            cg_update<T><<<nb, kThreads, 0, st>>>(static_cast<SV<T> *>(x), static_cast<SV<T> *>(r),
-                                                   static_cast<const SV<T> *>(p), static_cast<const SV<T> *>(Ap), s->sc,
-                                                   g.Vh, g.stride, s->partials);
+            launch_pdl(cg_update<T>, dim3(nb), kThreads, st, static_cast<SV<T> *>(x), static_cast<SV<T> *>(r),
+                       static_cast<const SV<T> *>(p), static_cast<const SV<T> *>(Ap), (const Scalars *)s->sc, g.Vh,
+                       g.stride, s->partials);
             count_launch();
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = finish_on(s, kBeta, st);
         if (e == cudaSuccess) {
-            cg_xpay<T><<<nb, kThreads, 0, st>>>(static_cast<const SV<T> *>(r), static_cast<SV<T> *>(p), s->sc, g.Vh,
-                                                 g.stride);
+            launch_pdl(cg_xpay<T>, dim3(nb), kThreads, st, static_cast<const SV<T> *>(r), static_cast<SV<T> *>(p),
+                       (const Scalars *)s->sc, g.Vh, g.stride);
             count_launch();
             e = cudaGetLastError();
         }
@@ -477,16 +487,16 @@ cudaError_t cg_h(gbds_solver s, double target_rr, int max_iter, int *iters, cuda
         if (e == cudaSuccess) e = finish_on(s, kAlpha, st);
         if (e == cudaSuccess) e = apply_M_h(s, s->Mp16, s->t16, s->Ap16, -1, nullptr, st);
         if (e == cudaSuccess) {
-            cg_update_h<FMT><<<nb, kThreads, 0, st>>>(static_cast<float4 *>(s->e32), static_cast<float4 *>(s->r32),
-                                                       static_cast<const char *>(s->p16), static_cast<const char *>(s->Ap16),
-                                                       s->sc, g.Vh, g.stride, s->partials);
+            launch_pdl(cg_update_h<FMT>, dim3(nb), kThreads, st, static_cast<float4 *>(s->e32),
+                       static_cast<float4 *>(s->r32), static_cast<const char *>(s->p16),
+                       static_cast<const char *>(s->Ap16), (const Scalars *)s->sc, g.Vh, g.stride, s->partials);
             count_launch();
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = finish_on(s, kBeta, st);
         if (e == cudaSuccess) {
-            cg_xpay_h<FMT><<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->r32), static_cast<char *>(s->p16), s->sc,
-                                                     g.Vh, g.stride);
+            launch_pdl(cg_xpay_h<FMT>, dim3(nb), kThreads, st, static_cast<const float4 *>(s->r32),
+                       static_cast<char *>(s->p16), (const Scalars *)s->sc, g.Vh, g.stride);
             count_launch();
             e = cudaGetLastError();
         }
@@ -914,6 +924,8 @@ enum BFinish { kBAlpha = 0, kBBeta = 1, kBSetRR = 2 };
 template <int NRHS>
 __global__ void __launch_bounds__(128) bcg_update(float4 *r, const float4 *__restrict__ Ap, const BScalars *sc, long long n,
                                                  size_t cs, double *partials) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = (int)(t % NRHS);
     float nrm = 0.f;
@@ -934,6 +946,8 @@ __global__ void __launch_bounds__(128) bcg_update(float4 *r, const float4 *__res
 template <int NRHS>
 __global__ void __launch_bounds__(128) bcg_xpay(float4 *x, const float4 *__restrict__ r, float4 *p, const BScalars *sc,
                                                long long n, size_t cs) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int q = (int)(t % NRHS);
@@ -965,6 +979,8 @@ __global__ void __launch_bounds__(128) bnorm(const float4 *__restrict__ v, long 
 // (thread t takes rhs t % nrhs: coalesced reads) into partials2[j][rhs].
 constexpr int kBRows = 1024;  // partial rows per stage-1 block
 __global__ void __launch_bounds__(256) bfinish1(const double *partials, int nrows, int nrhs, double *partials2) {
+    pdl_allow_next();
+    pdl_wait_prev();
     __shared__ double buf[256];
     const int q = threadIdx.x % nrhs, lanes = 256 / nrhs;  // nrhs divides 256
     const int row0 = blockIdx.x * kBRows;
@@ -983,6 +999,8 @@ __global__ void __launch_bounds__(256) bfinish1(const double *partials, int nrow
 // Stage 2: per rhs (thread), the sum over the stage-1 blocks, then the
 // scalar step.
 __global__ void __launch_bounds__(32) bfinish2(const double *partials2, int nblocks2, int nrhs, BScalars *sc, int mode) {
+    pdl_allow_next();
+    pdl_wait_prev();
     const int q = threadIdx.x;
     if (q >= nrhs) return;
     double sum = 0;
@@ -1090,8 +1108,8 @@ size_t bcs(gbds_bsolver b) { return (size_t)b->s1->g.stride * b->nrhs; }
 int bblocks2(gbds_bsolver b) { return (bblocks(b) + kBRows - 1) / kBRows; }
 
 cudaError_t bfinish_on(gbds_bsolver b, int mode, cudaStream_t st) {
-    bfinish1<<<bblocks2(b), 256, 0, st>>>(b->bpartials, bblocks(b), b->nrhs, b->bpartials2);
-    bfinish2<<<1, 32, 0, st>>>(b->bpartials2, bblocks2(b), b->nrhs, b->bsc, mode);
+    launch_pdl(bfinish1, dim3(bblocks2(b)), 256, st, b->bpartials, bblocks(b), b->nrhs, b->bpartials2);
+    launch_pdl(bfinish2, dim3(1), 32, st, b->bpartials2, bblocks2(b), b->nrhs, b->bsc, mode);
     count_launch(2);
     return cudaGetLastError();
 }
@@ -1136,8 +1154,8 @@ cudaError_t bcg(gbds_bsolver b, const std::vector<double> &target, int max_iter,
         if (e == cudaSuccess) e = apply_Mb(b, b->Mp, b->Ap, -1, nullptr, st);
         if (e == cudaSuccess) {
 #define GBDS_UPD(NR)                                                                                      \
-    bcg_update<NR><<<nb, 128, 0, st>>>(static_cast<float4 *>(b->r), static_cast<const float4 *>(b->Ap), b->bsc, n, \
-                                       cs, b->bpartials)
+    launch_pdl(bcg_update<NR>, dim3(nb), 128, st, static_cast<float4 *>(b->r), static_cast<const float4 *>(b->Ap), \
+               (const BScalars *)b->bsc, n, cs, b->bpartials)
             GBDS_BN(nr, GBDS_UPD)
 #undef GBDS_UPD
             count_launch();
@@ -1146,8 +1164,8 @@ cudaError_t bcg(gbds_bsolver b, const std::vector<double> &target, int max_iter,
         if (e == cudaSuccess) e = bfinish_on(b, kBBeta, st);
         if (e == cudaSuccess) {
 #define GBDS_XP(NR)                                                                                         \
-    bcg_xpay<NR><<<nb, 128, 0, st>>>(static_cast<float4 *>(b->e), static_cast<const float4 *>(b->r),               \
-                                     static_cast<float4 *>(b->p), b->bsc, n, cs)
+    launch_pdl(bcg_xpay<NR>, dim3(nb), 128, st, static_cast<float4 *>(b->e), static_cast<const float4 *>(b->r), \
+               static_cast<float4 *>(b->p), (const BScalars *)b->bsc, n, cs)
             GBDS_BN(nr, GBDS_XP)
 #undef GBDS_XP
             count_launch();
