@@ -148,6 +148,13 @@ int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity, void *psi_
  * GBDS_SUCCESS), as in the reference.  cb must be 0 or 1. */
 int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
                    int isign, int cb, void *stream);
+/* Stream ordering: the Dslash and solver kernels use programmatic dependent
+ * launch.  Each waits (griddepcontrol.wait) for the previous grid on its
+ * stream before its first global read, and lets the next grid launched with
+ * cudaLaunchAttributeProgrammaticStreamSerialization start early.  Kernels
+ * launched without that attribute, copies and events are ordered as usual.
+ * A caller kernel launched with the attribute after one of these must itself
+ * wait (cudaGridDependencySynchronize) before reading their output. */
 
 /* Launch tuning of gbds_op_dslash: threads per block (0 = default 128; a
  * multiple of 32 up to 256) and a kernel variant.  Single rhs: 0 = registers

@@ -370,7 +370,9 @@ void launch_pdl(void (*kernel)(P...), dim3 grid, int block, cudaStream_t stream,
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, args...);
+    // a failed launch also sets the runtime's last error, which every
+    // launcher returns through cudaGetLastError()
+    (void)cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
 template <typename T, int MINB>
