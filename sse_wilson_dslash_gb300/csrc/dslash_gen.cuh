@@ -205,6 +205,13 @@ __device__ __forceinline__ void load_link_g(const char *base, int stride, int h,
     }
 }
 
+// Per-rhs scalars of the batched CG, read by the fused update epilogue.
+struct RhsCgScalars {
+    double rr, pAp, alpha, beta;
+    int active;
+    int pad;
+};
+
 struct GenArgs {
     Geom g;
     const char *psi;           // source checkerboard
@@ -218,6 +225,11 @@ struct GenArgs {
     const char *x;
     float coef;
     double *partials;
+    // fused CG update (fully packed kernel, FP32 spin pairs): instead of
+    // storing v = x + coef * D psi, r -= alpha_r v for active rhs, with
+    // per-(block, rhs) |r|^2 partials
+    const RhsCgScalars *rsc;
+    float4 *rvec;
 };
 
 // NRHS > 0: compile-time count; NRHS == 0: a.nrhs at run time.
@@ -609,22 +621,47 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
             acc[3][c] = {LR[c].y, LI[c].y};
         }
         const size_t i = (size_t)h * NRHS + r;
-        if constexpr (EPI) {
-            cx<float> xv[4][3];
-            Sio<FMT>::load(a.x, a.cs, i, xv);
+        if constexpr (EPI == 3) {
+            static_assert(FMT == kFmtF32Pairs, "the fused CG update works on FP32 spin pairs");
+            const RhsCgScalars &sq = a.rsc[r];
+            if (sq.active) {
+                cx<float> xv[4][3];
+                Sio<FMT>::load(a.x, a.cs, i, xv);
+                const float al = (float)sq.alpha;
 #pragma unroll
-            for (int s = 0; s < 4; s++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    acc[s][c].r = fmaf(a.coef, acc[s][c].r, xv[s][c].r);
-                    acc[s][c].i = fmaf(a.coef, acc[s][c].i, xv[s][c].i);
-                    nrm = fmaf(acc[s][c].r, acc[s][c].r, nrm);
-                    nrm = fmaf(acc[s][c].i, acc[s][c].i, nrm);
+                for (int k = 0; k < 6; k++) {
+                    const int s0 = k < 3 ? 0 : 2, c = k % 3;
+                    // v in the spin-pair component order of float4 k
+                    const float4 v = make_float4(fmaf(a.coef, acc[s0][c].r, xv[s0][c].r),
+                                                 fmaf(a.coef, acc[s0 + 1][c].r, xv[s0 + 1][c].r),
+                                                 fmaf(a.coef, acc[s0][c].i, xv[s0][c].i),
+                                                 fmaf(a.coef, acc[s0 + 1][c].i, xv[s0 + 1][c].i));
+                    float4 *rp = a.rvec + (size_t)k * a.cs + i;
+                    const float4 ro = *rp;
+                    const float4 rn = make_float4(fmaf(-al, v.x, ro.x), fmaf(-al, v.y, ro.y), fmaf(-al, v.z, ro.z),
+                                                  fmaf(-al, v.w, ro.w));
+                    *rp = rn;
+                    nrm += rn.x * rn.x + rn.y * rn.y + rn.z * rn.z + rn.w * rn.w;
                 }
+            }
+        } else {
+            if constexpr (EPI) {
+                cx<float> xv[4][3];
+                Sio<FMT>::load(a.x, a.cs, i, xv);
+#pragma unroll
+                for (int s = 0; s < 4; s++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        acc[s][c].r = fmaf(a.coef, acc[s][c].r, xv[s][c].r);
+                        acc[s][c].i = fmaf(a.coef, acc[s][c].i, xv[s][c].i);
+                        nrm = fmaf(acc[s][c].r, acc[s][c].r, nrm);
+                        nrm = fmaf(acc[s][c].i, acc[s][c].i, nrm);
+                    }
+            }
+            Sio<FMT>::store(a.res, a.cs, i, acc);
         }
-        Sio<FMT>::store(a.res, a.cs, i, acc);
     }
-    if constexpr (EPI == 2) {
+    if constexpr (EPI >= 2) {
         if (a.partials) block_sum_rhs<NRHS>(a.partials, nrm);
     }
 }

@@ -7,6 +7,11 @@ cudaError_t launch_gen_f32p(const Geom &g, int recon, int nrhs, const void *gaug
                             int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant) {
     return launch_gen_t<kFmtF32Pairs>(g, recon, nrhs, gauge, psi, res, isign, cb, x, coef, partials, st, variant);
 }
+cudaError_t launch_gen_f32p_cg_update(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, int isign,
+                                      int cb, const void *x, float coef, const RhsCgScalars *rsc, void *r,
+                                      double *partials, cudaStream_t st) {
+    return launch_gen_cg_update_t<kFmtF32Pairs>(g, recon, nrhs, gauge, psi, isign, cb, x, coef, rsc, r, partials, st);
+}
 cudaError_t launch_pack_gen_f32p(const Geom &g, int nrhs, const float *packed, const int *table, int parity, void *out,
                                  cudaStream_t st) {
     return launch_pack_gen_t<kFmtF32Pairs>(g, nrhs, packed, table, parity, out, st);

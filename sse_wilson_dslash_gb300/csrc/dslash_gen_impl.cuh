@@ -158,6 +158,39 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     return cudaGetLastError();
 }
 
+// The batched CG's fused update (fully packed kernel, FP32 spin pairs, nrhs
+// 8, 16 or 32): r -= alpha_r (x + coef D psi) for the active rhs of rsc,
+// with per-(128-element block, rhs) |r|^2 partials; nothing else is stored.
+template <int FMT>
+cudaError_t launch_gen_cg_update_t(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, int isign,
+                                   int cb, const void *x, float coef, const RhsCgScalars *rsc, void *r, double *partials,
+                                   cudaStream_t st) {
+    if (nrhs != 8 && nrhs != 16 && nrhs != 32) return cudaErrorInvalidValue;
+    GenArgs a;
+    a.g = g;
+    a.psi = static_cast<const char *>(psi);
+    a.res = nullptr;
+    a.gauge = static_cast<const char *>(gauge);
+    a.link_block_bytes = (size_t)recon * 4 * g.stride;
+    a.cs = (size_t)g.stride * nrhs;
+    a.nrhs = nrhs;
+    a.pt = 1 - cb;
+    a.x = static_cast<const char *>(x);
+    a.coef = coef;
+    a.partials = partials;
+    a.rsc = rsc;
+    a.rvec = static_cast<float4 *>(r);
+    if (recon == 18) {
+        if (isign > 0) launch_gen3_nrhs<FMT, 18, 1, 3>(a, nrhs, st);
+        else launch_gen3_nrhs<FMT, 18, -1, 3>(a, nrhs, st);
+    } else {
+        if (isign > 0) launch_gen3_nrhs<FMT, 12, 1, 3>(a, nrhs, st);
+        else launch_gen3_nrhs<FMT, 12, -1, 3>(a, nrhs, st);
+    }
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <int FMT>
 cudaError_t launch_pack_gen_t(const Geom &g, int nrhs, const float *packed, const int *table, int parity, void *out,
                               cudaStream_t st) {

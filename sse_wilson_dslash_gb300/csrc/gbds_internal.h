@@ -79,6 +79,13 @@ cudaError_t launch_pack_gen_half(int fmt, const Geom &g, int nrhs, const float *
                                  void *out, cudaStream_t st);
 cudaError_t launch_unpack_gen_half(int fmt, const Geom &g, int nrhs, const void *in, const int *table, int parity,
                                    float *packed, cudaStream_t st);
+// The batched CG's fused update on FP32 spin pairs (nrhs 8, 16, 32):
+// r -= alpha_q (x + coef D psi) for the active rhs q of rsc, per-(128-element
+// block, rhs) |r|^2 partials; nothing else is stored.
+struct RhsCgScalars;
+cudaError_t launch_gen_f32p_cg_update(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, int isign,
+                                      int cb, const void *x, float coef, const RhsCgScalars *rsc, void *r,
+                                      double *partials, cudaStream_t st);
 inline int gen_spinor_bytes(int fmt) { return (fmt == 0 || fmt == 3) ? 96 : (fmt == 1 ? 48 : 52); }
 // Tensor-core form (dslash_tc.cu): fmt 1 / 2, nrhs 16 or 32, FP32 links
 // converted to the 16-bit operand type; err set to 1 on a timed-out wait.

@@ -911,11 +911,7 @@ static int solve_impl(gbds_solver s, const double *b_packed, double *x_packed, g
 namespace gbds {
 namespace {
 
-struct BScalars {
-    double rr, pAp, alpha, beta;
-    int active;
-    int pad;
-};
+using BScalars = RhsCgScalars;  // rr, pAp, alpha, beta, active (dslash_gen.cuh)
 
 enum BFinish { kBAlpha = 0, kBBeta = 1, kBSetRR = 2 };
 
@@ -1127,6 +1123,21 @@ cudaError_t apply_Mb(gbds_bsolver b, const void *in, void *out, int isign, doubl
     return launch_gen_f32p(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, out, isign, 1, in, -k2, partials, st, v);
 }
 
+// The fully packed operator (16, 32 rhs) fuses the CG's r -= alpha Ap into
+// M^+'s second launch: Ap is never stored.
+bool fused_update(gbds_bsolver b) { return b->nrhs == 16 || b->nrhs == 32; }
+
+// r -= alpha_r M^+ in for all active rhs, per-rhs |r|^2 partials
+cudaError_t apply_Mb_dagger_update(gbds_bsolver b, const void *in, cudaStream_t st) {
+    gbds_solver s = b->s1;
+    const float k2 = (float)(s->prm.kappa * s->prm.kappa);
+    cudaError_t e =
+        launch_gen_f32p(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, -1, 0, nullptr, 0.f, nullptr, st, 2);
+    if (e != cudaSuccess) return e;
+    return launch_gen_f32p_cg_update(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, -1, 1, in, -k2, b->bsc, b->r,
+                                     b->bpartials, st);
+}
+
 cudaError_t read_bscalars(gbds_bsolver b, cudaStream_t st) {
     cudaError_t e = cudaMemcpyAsync(b->hbsc, b->bsc, sizeof(BScalars) * b->nrhs, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1151,8 +1162,12 @@ cudaError_t bcg(gbds_bsolver b, const std::vector<double> &target, int max_iter,
         if (!any) break;
         e = apply_Mb(b, b->p, b->Mp, +1, b->bpartials, st);
         if (e == cudaSuccess) e = bfinish_on(b, kBAlpha, st);
-        if (e == cudaSuccess) e = apply_Mb(b, b->Mp, b->Ap, -1, nullptr, st);
-        if (e == cudaSuccess) {
+        if (e == cudaSuccess && fused_update(b)) {
+            e = apply_Mb_dagger_update(b, b->Mp, st);
+        } else if (e == cudaSuccess) {
+            e = apply_Mb(b, b->Mp, b->Ap, -1, nullptr, st);
+        }
+        if (e == cudaSuccess && !fused_update(b)) {
 #define GBDS_UPD(NR)                                                                                      \
     launch_pdl(bcg_update<NR>, dim3(nb), 128, st, static_cast<float4 *>(b->r), static_cast<const float4 *>(b->Ap), \
                (const BScalars *)b->bsc, n, cs, b->bpartials)
@@ -1230,9 +1245,10 @@ extern "C" int gbds_bsolver_create(gbds_bsolver *out, const int dims[4], int nrh
         v->assign(nrhs, nullptr);
         for (int q = 0; q < nrhs && e == cudaSuccess; q++) e = cudaMalloc(&(*v)[q], f64);
     }
-    void **bufs[] = {&b->e, &b->r, &b->p, &b->Ap, &b->Mp, &b->t};
+    void **bufs[] = {&b->e, &b->r, &b->p, &b->Mp, &b->t};
     for (void **x : bufs)
         if (e == cudaSuccess) e = cudaMalloc(x, f32m);
+    if (e == cudaSuccess && !fused_update(b)) e = cudaMalloc(&b->Ap, f32m);  // else never stored
     if (e == cudaSuccess) e = cudaMalloc(&b->bpartials, sizeof(double) * (size_t)bblocks(b) * nrhs);
     if (e == cudaSuccess) e = cudaMalloc(&b->bpartials2, sizeof(double) * (size_t)bblocks2(b) * nrhs);
     if (e == cudaSuccess) e = cudaMalloc(&b->bsc, sizeof(BScalars) * nrhs);

@@ -84,13 +84,14 @@ def test_mixed_and_fp64_solutions_agree():
         assert (xs[0] - x).norm() / xs[0].norm() < 1e-9
 
 
-@pytest.mark.parametrize("nrhs,inner_recon", [(4, 12), (8, 18)])
+@pytest.mark.parametrize("nrhs,inner_recon", [(4, 12), (8, 18), (16, 12), (32, 18)])
 def test_batched_solve_matches_single_solves(nrhs, inner_recon):
     """The batched solver: every right-hand side reaches 1e-10, its solution
     agrees with the single-rhs mixed solve of the same system, and the
     oracle confirms |b - M x| / |b|.  One right-hand side is zero (its
     solution stays zero) and two are multiples of each other (their
-    solutions are the same multiples)."""
+    solutions are the same multiples).  16 and 32 right-hand sides run the
+    fully packed operator with the CG's r update fused into M^+."""
     import torch
     from sse_wilson_dslash_gb300.device import BatchedWilsonSolver, WilsonSolver
     dims = (8, 8, 8, 8)
