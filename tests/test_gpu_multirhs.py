@@ -112,10 +112,11 @@ def test_tensor_cores_need_16bit_and_16_or_32_rhs():
         op.close()
 
 
-@pytest.mark.parametrize("fmt", ["bf16", "f16"])
+@pytest.mark.parametrize("fmt", ["bf16", "f16", "f32_pairs"])
 def test_autotune_chooses_between_cuda_and_tensor_cores(fmt):
-    """The autotuner times both kernels for a 16-bit, 32-rhs operator; the
-    pick (cached) gives the same answer as the oracle."""
+    """The autotuner times the CUDA-core variants (and, for 16-bit storage,
+    the tensor-core kernel) for a 32-rhs operator; the pick (cached) gives the
+    same answer as the oracle."""
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
     dims, nrhs = (8, 8, 8, 8), 32
