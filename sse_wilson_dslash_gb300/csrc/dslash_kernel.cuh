@@ -97,6 +97,32 @@ __device__ __forceinline__ void su3_mul(const cx<T> (&U)[3][3], const cx<T> (&h)
     }
 }
 
+// w_k += U h_k (DAG = false) or U^dagger h_k (DAG = true): the FMA chains
+// start from w.
+template <bool DAG, typename T>
+__device__ __forceinline__ void su3_mul_acc(const cx<T> (&U)[3][3], const cx<T> (&h)[2][3], cx<T> (&w)[2][3]) {
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            T re = w[k][i].r, im = w[k][i].i;
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const cx<T> m = DAG ? U[j][i] : U[i][j];
+                const cx<T> v = h[k][j];
+                if (DAG) {
+                    re = fma(m.r, v.r, re); re = fma(m.i, v.i, re);
+                    im = fma(m.r, v.i, im); im = fma(-m.i, v.r, im);
+                } else {
+                    re = fma(m.r, v.r, re); re = fma(-m.i, v.i, re);
+                    im = fma(m.r, v.i, im); im = fma(m.i, v.r, im);
+                }
+            }
+            w[k][i] = {re, im};
+        }
+    }
+}
+
 // Third row of an SU(3) matrix from the first two: row2 = conj(row0 x row1).
 template <typename T>
 __device__ __forceinline__ void reconstruct_row2(cx<T> (&U)[3][3]) {
@@ -319,6 +345,49 @@ __device__ __forceinline__ void hop_pair(const DslashArgs<T> &a, int h, const Nb
     reconstruct<MU, -ISIGN>(acc, w);
 }
 
+// FP64 (issue-bound on the FP64 pipe): the backward coefficients of the lower
+// spin components are the forward ones negated, so with S = w_f + w_b (the
+// backward product's FMA chains start from w_f) and D = w_f - w_b = 2 w_f - S
+// the hop pair adds S to the upper and c D to the lower components: 12 fewer
+// FP64 operations per direction than two separate reconstructions.
+template <int ND, int RECON, int ISIGN, int MU>
+__device__ __forceinline__ void hop_pair_sd(const DslashArgs<double> &a, int h, const Nbr &n, cx<double> (&acc)[4][3]) {
+    using F = Field<double>;
+    using P = Proj<MU>;
+    constexpr int f = ISIGN > 0 ? 0 : 1;  // the forward hop's sign flip
+    const int ps = 1 - a.pt;
+    cx<double> s[4][3], hs[2][3], w[2][3], U[3][3];
+    F::load_spinor(a.psi, a.g.stride, n.f[MU], s);
+    F::template load_link<RECON, true>(a.gauge + (size_t)(a.pt * ND + MU) * a.link_block_bytes, a.g.stride, h, U);
+    project<MU, ISIGN>(s, hs);
+    su3_mul<false>(U, hs, w);
+    cx<double> wf[2][3];
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) wf[k][c] = w[k][c];
+    F::load_spinor(a.psi, a.g.stride, n.b[MU], s);
+    F::template load_link<RECON, true>(a.gauge + (size_t)(ps * ND + MU) * a.link_block_bytes, a.g.stride, n.b[MU], U);
+    project<MU, -ISIGN>(s, hs);
+    su3_mul_acc<true>(U, hs, w);  // w = S
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        cx<double> d[2];
+#pragma unroll
+        for (int k = 0; k < 2; k++) d[k] = {fma(2.0, wf[k][c].r, -w[k][c].r), fma(2.0, wf[k][c].i, -w[k][c].i)};
+        acc[0][c] = cadd(acc[0][c], w[0][c]);
+        acc[1][c] = cadd(acc[1][c], w[1][c]);
+        acc[2][c] = cadd(acc[2][c], mulc<P::b2 ^ f>(d[P::k2]));
+        acc[3][c] = cadd(acc[3][c], mulc<P::b3 ^ f>(d[P::k3]));
+    }
+}
+
+template <typename T, int ND, int RECON, int ISIGN, int MU>
+__device__ __forceinline__ void hop_pair_any(const DslashArgs<T> &a, int h, const Nbr &n, cx<T> (&acc)[4][3]) {
+    if constexpr (sizeof(T) == 8) hop_pair_sd<ND, RECON, ISIGN, MU>(a, h, n, acc);
+    else hop_pair<T, ND, RECON, ISIGN, MU>(a, h, n, acc);
+}
+
 // MINB > 0 caps registers so that MINB blocks of 128 threads fit on an SM
 // (launch with 128 threads); MINB == 0 leaves registers uncapped (<= 256 threads).
 template <int MINB> struct Bounds { static constexpr int threads = 128, blocks = MINB; };
@@ -345,10 +414,10 @@ __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks) d
     for (int s = 0; s < 4; s++)
 #pragma unroll
         for (int c = 0; c < 3; c++) acc[s][c] = {T(0), T(0)};
-    hop_pair<T, ND, RECON, ISIGN, 0>(a, h, n, acc);
-    hop_pair<T, ND, RECON, ISIGN, 1>(a, h, n, acc);
-    hop_pair<T, ND, RECON, ISIGN, 2>(a, h, n, acc);
-    if constexpr (ND == 4) hop_pair<T, ND, RECON, ISIGN, 3>(a, h, n, acc);
+    hop_pair_any<T, ND, RECON, ISIGN, 0>(a, h, n, acc);
+    hop_pair_any<T, ND, RECON, ISIGN, 1>(a, h, n, acc);
+    hop_pair_any<T, ND, RECON, ISIGN, 2>(a, h, n, acc);
+    if constexpr (ND == 4) hop_pair_any<T, ND, RECON, ISIGN, 3>(a, h, n, acc);
     Field<T>::store_spinor(a.res, a.g.stride, h, acc);
 }
 
@@ -432,10 +501,10 @@ __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks)
         for (int s = 0; s < 4; s++)
 #pragma unroll
             for (int c = 0; c < 3; c++) acc[s][c] = {T(0), T(0)};
-        hop_pair<T, 4, RECON, ISIGN, 0>(a, h, n, acc);
-        hop_pair<T, 4, RECON, ISIGN, 1>(a, h, n, acc);
-        hop_pair<T, 4, RECON, ISIGN, 2>(a, h, n, acc);
-        hop_pair<T, 4, RECON, ISIGN, 3>(a, h, n, acc);
+        hop_pair_any<T, 4, RECON, ISIGN, 0>(a, h, n, acc);
+        hop_pair_any<T, 4, RECON, ISIGN, 1>(a, h, n, acc);
+        hop_pair_any<T, 4, RECON, ISIGN, 2>(a, h, n, acc);
+        hop_pair_any<T, 4, RECON, ISIGN, 3>(a, h, n, acc);
         cx<T> xv[4][3];
         load_spinor_any<T>(x, a.g.stride, h, xv);
 #pragma unroll
