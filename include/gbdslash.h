@@ -61,7 +61,7 @@ typedef enum gbds_status {
     GBDS_ERROR_NOT_INITIALIZED = 2, /* handle or legacy state not set up            */
     GBDS_ERROR_CUDA = 3,            /* a CUDA runtime call failed                   */
     GBDS_ERROR_OUT_OF_MEMORY = 4,   /* device or pinned host allocation failed      */
-    GBDS_ERROR_UNSUPPORTED = 5      /* valid request this build does not implement  */
+    GBDS_ERROR_UNSUPPORTED = 5      /* valid request the library does not implement */
 } gbds_status;
 
 /* Storage precisions and gauge compressions. */
