@@ -65,6 +65,40 @@ def test_multi_rhs_bytes_accounting():
     op.close()
 
 
+@pytest.mark.parametrize("fmt", ["native", "f32_pairs"])
+def test_fp32_field_layouts_match_the_header(fmt):
+    """The packed bytes of the two FP32 multi-rhs formats are the layouts
+    include/gbdslash.h documents: element (k, h, r) at
+    k*stride*nrhs + h*nrhs + r, 16-byte component k holding complex elements
+    2k and 2k+1 (FP32), or (s0c.r, s1c.r, s0c.i, s1c.i) for k = c < 3 and
+    (s2c.r, s3c.r, s2c.i, s3c.i) for k = 3 + c (FP32 spin pairs)."""
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims, nrhs = (4, 4, 4, 4), 2
+    op = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
+    V, Vh, stride = op.volume, op.volume_cb, op.stride
+    # value = r * 100000 + site * 100 + spin * 10 + colour * 2 + reim: exact in FP32
+    r_, site, spin, col, ri = np.meshgrid(np.arange(nrhs), np.arange(V), np.arange(4), np.arange(3), np.arange(2),
+                                          indexing="ij")
+    psi = (r_ * 100000 + site * 100 + spin * 10 + col * 2 + ri).astype(np.float32)
+    for parity in (0, 1):
+        raw = op.pack_spinor(torch.from_numpy(psi.ravel()).cuda(), parity)
+        got = raw.view(torch.float32).cpu().numpy().reshape(6, stride, nrhs, 4)[:, :Vh]
+        s = psi[:, parity * Vh:(parity + 1) * Vh].transpose(1, 0, 2, 3, 4)  # [h][r][spin][colour][reim]
+        want = np.empty((6, Vh, nrhs, 4), dtype=np.float32)
+        for k in range(6):
+            if fmt == "native":
+                e0, e1 = 2 * k, 2 * k + 1
+                want[k] = np.stack([s[:, :, e0 // 3, e0 % 3, 0], s[:, :, e0 // 3, e0 % 3, 1],
+                                    s[:, :, e1 // 3, e1 % 3, 0], s[:, :, e1 // 3, e1 % 3, 1]], axis=-1)
+            else:
+                a, c = (0, k) if k < 3 else (2, k - 3)
+                want[k] = np.stack([s[:, :, a, c, 0], s[:, :, a + 1, c, 0], s[:, :, a, c, 1], s[:, :, a + 1, c, 1]],
+                                   axis=-1)
+        np.testing.assert_array_equal(got, want)
+    op.close()
+
+
 # Tensor-core form: besides the storage rounding above, the projected half
 # spinor and the link enter the MMA rounded to the 16-bit operand type (one
 # more rounding of each, FP32 accumulation), well inside the same per-site
