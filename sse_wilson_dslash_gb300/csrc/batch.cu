@@ -83,6 +83,8 @@ __device__ __forceinline__ void batch_site(const Problem &P, int t) {
 template <int FMT, int RECON>
 __global__ void __launch_bounds__(256, 3) batch_kernel(const __grid_constant__ BatchParams bp, const Tile *__restrict__ tiles,
                                                     int ntiles) {
+    pdl_allow_next();
+    pdl_wait_prev();
     for (int w = blockIdx.x; w < ntiles; w += gridDim.x) {
         const Tile tl = tiles[w];
         const Problem &P = bp.p[tl.problem];
@@ -158,7 +160,7 @@ int build_tiles(gbds_batch b) {
 cudaError_t launch_batch(gbds_batch b, cudaStream_t st) {
     int grid = b->grid > 0 ? b->grid : b->ntiles;
     grid = std::max(1, std::min(grid, b->ntiles));
-#define GBDS_B(F, R) batch_kernel<F, R><<<grid, b->block, 0, st>>>(b->params, b->d_tiles, b->ntiles)
+#define GBDS_B(F, R) launch_pdl(batch_kernel<F, R>, dim3(grid), b->block, st, b->params, (const Tile *)b->d_tiles, b->ntiles)
     if (b->recon == 18) {
         if (b->format == 0) GBDS_B(kFmtNative, 18); else if (b->format == 1) GBDS_B(kFmtBF16, 18);
         else if (b->format == 2) GBDS_B(kFmtF16N, 18); else GBDS_B(kFmtF32Pairs, 18);
