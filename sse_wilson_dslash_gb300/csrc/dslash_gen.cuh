@@ -597,9 +597,9 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
 #define GBDS_G3_HOP(MU, LORD)                                                                            \
     {                                                                                                    \
         float v[24];                                                                                     \
-        float sc = load_reals<FMT>(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, v);                        \
+        float sc = load_reals<FMT>(a.psi, a.cs, (size_t)n.f[MU] * NRHS + r, v);                          \
         packed_hop<MU, ISIGN, LORD, SCALE>(v, sc, sL[p][2 * MU], UR, UI, LR, LI);                        \
-        sc = load_reals<FMT>(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, v);                              \
+        sc = load_reals<FMT>(a.psi, a.cs, (size_t)n.b[MU] * NRHS + r, v);                                \
         packed_hop<MU, -ISIGN, LORD, SCALE>(v, sc, sL[p][2 * MU + 1], UR, UI, LR, LI);                   \
     }
         GBDS_G3_HOP(0, 1)
