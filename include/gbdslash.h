@@ -116,9 +116,11 @@ int gbds_op_nrhs(gbds_op op);
 int gbds_op_set_tensor_cores(gbds_op op, int on);
 int gbds_op_check(gbds_op op);
 /* Diagnostic: runs the tensor-core kernel's bounded mbarrier wait, with
- * `polls` polls, on a barrier that nothing completes, and returns
- * GBDS_SUCCESS when the wait gave up and reported it (the context stays
- * usable).  No reference counterpart. */
+ * `polls` polls, on a barrier that nothing completes, then the bounded drain
+ * the kernel runs before it releases its tensor memory (4 more waits of
+ * `polls` polls), and returns GBDS_SUCCESS when both gave up and reported the
+ * code of MMAs that never completed (the context stays usable).  No
+ * reference counterpart. */
 int gbds_tc_wait_selftest(int polls);
 
 /* Caller site layout for pack/unpack: site_table[i] = caller linear index of
@@ -148,8 +150,8 @@ int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity, void *psi_
  * GBDS_SUCCESS), as in the reference.  cb must be 0 or 1. */
 int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
                    int isign, int cb, void *stream);
-/* Stream ordering: the Dslash and solver kernels use programmatic dependent
- * launch.  Each waits (griddepcontrol.wait) for the previous grid on its
+/* Stream ordering: the Dslash, solver and uneven-batch kernels use
+ * programmatic dependent launch.  Each waits (griddepcontrol.wait) for the previous grid on its
  * stream before its first global read, and lets the next grid launched with
  * cudaLaunchAttributeProgrammaticStreamSerialization start early.  Kernels
  * launched without that attribute, copies and events are ordered as usual.

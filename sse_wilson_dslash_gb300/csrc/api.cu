@@ -205,6 +205,9 @@ extern "C" int gbds_op_check(gbds_op op) {
     if (e != cudaSuccess) return cuda_error(e, "gbds_op_check");
     if (v) {
         cudaMemset(op->d_err, 0, sizeof(int));
+        if (v == 2)
+            return set_error(GBDS_ERROR_CUDA, "a tensor-core Dslash launch timed out waiting for its MMAs, which "
+                                              "had still not completed when its tensor memory was released");
         return set_error(GBDS_ERROR_CUDA, "a tensor-core Dslash launch timed out waiting for its MMAs");
     }
     return GBDS_SUCCESS;
@@ -221,7 +224,7 @@ extern "C" int gbds_tc_wait_selftest(int polls) {
     if (e == cudaSuccess) e = cudaMemcpy(&flag, d, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return cuda_error(e, "gbds_tc_wait_selftest");
-    return flag == 1 ? GBDS_SUCCESS : set_error(GBDS_ERROR_CUDA, "the bounded wait did not report its time-out");
+    return flag == 2 ? GBDS_SUCCESS : set_error(GBDS_ERROR_CUDA, "the bounded wait did not report its time-out");
 }
 
 extern "C" size_t gbds_op_gauge_bytes(gbds_op op) { return op ? gauge_bytes(op->g, op->prec, op->recon) : 0; }

@@ -215,7 +215,7 @@ extern "C" int gbds_batch_create(gbds_batch *out, const gbds_batch_item *items, 
     for (int i = 0; i < n; i++) b->params.p[i] = b->probs[i];
     int rc = build_tiles(b);
     if (rc != GBDS_SUCCESS) {
-        delete b;
+        gbds_batch_destroy(b);  // frees a tile list that was allocated before the failing copy
         return rc;
     }
     *out = b;
@@ -287,8 +287,10 @@ extern "C" int gbds_batch_autotune(gbds_batch b, void *stream) {
     float best = 1e30f;
     int pick[3] = {b->block, b->grid, b->order};
     cudaError_t e = cudaSuccess;
-    for (int blk : {64, 128, 256})
-        for (int mult : {2, 4, 6, 8})
+    // every (tile size, resident CTAs, order) candidate; the first CUDA error
+    // ends the whole search
+    for (int blk : {64, 128, 256}) {
+        for (int mult : {2, 4, 6, 8}) {
             for (int order : {0, 1}) {
                 int rc = gbds_batch_set_schedule(b, blk, b->sms * mult * 128 / blk, order);
                 if (rc != GBDS_SUCCESS) continue;
@@ -307,6 +309,10 @@ extern "C" int gbds_batch_autotune(gbds_batch b, void *stream) {
                     pick[2] = order;
                 }
             }
+            if (e != cudaSuccess) break;
+        }
+        if (e != cudaSuccess) break;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_error(e, "gbds_batch_autotune");

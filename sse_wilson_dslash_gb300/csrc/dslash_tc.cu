@@ -465,6 +465,15 @@ __device__ __forceinline__ bool wait_parity(uint32_t mbar, uint32_t parity, int 
     return done != 0;
 }
 
+// After a bounded wait that ran out: keep waiting for the same phase in up to
+// `rounds` more bounded waits.  Returns the error code to record: 1 if the
+// phase completed within them, 2 if it never did.
+__device__ __forceinline__ int drain_after_timeout(uint32_t mbar, uint32_t parity, int polls, int rounds) {
+    for (int r = 0; r < rounds; r++)
+        if (wait_parity(mbar, parity, polls)) return 1;
+    return 2;
+}
+
 template <int FMT, int RECON, int ISIGN, int NRHS>
 __global__ void __launch_bounds__(128, 512 / TcShape<NRHS>::COLS) dslash_tc_kernel(const __grid_constant__ TcArgs a) {
     using S = TcShape<NRHS>;
@@ -568,10 +577,13 @@ __global__ void __launch_bounds__(128, 512 / TcShape<NRHS>::COLS) dslash_tc_kern
         co = nco;
     }
     if (bad && t == 0) {
-        atomicExch(a.err, 1);
-        // the MMAs whose wait ran out may still be in flight: wait once more
-        // (bounded) before their columns are freed
-        wait_parity(mb, phase ^ 1u);
+        // The MMAs whose wait ran out may still be in flight, and their
+        // columns must not be freed under them.  Keep waiting, in bounded
+        // rounds (16 more rounds of 2^20 polls at most), and record 2 instead
+        // of 1 when they never completed.  The columns are freed in either
+        // case: a CTA must release its TMEM before it exits, and columns it
+        // kept would block every later tcgen05.alloc on this SM.
+        atomicMax(a.err, drain_after_timeout(mb, phase ^ 1u, 1 << 20, 16));
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -615,8 +627,10 @@ cudaError_t launch_tc_t(TcArgs a, cudaStream_t st) {
 }
 
 // A wait that nothing completes: an mbarrier that no thread or copy arrives
-// on.  flag = 1 when the bounded wait gave up (as the Dslash kernel's waits
-// do), 0 if it (wrongly) saw the phase complete.
+// on.  The kernel's two steps after a timed-out MMA wait run on it: the
+// bounded wait gives up, then the bounded drain gives up too.  flag = the code
+// the Dslash kernel would record (2: the phase never completed), 0 if the
+// first wait (wrongly) saw the phase complete.
 __global__ void tc_wait_selftest_kernel(int polls, int *flag) {
     __shared__ __align__(8) uint64_t bar;
     if (threadIdx.x == 0) {
@@ -625,7 +639,8 @@ __global__ void tc_wait_selftest_kernel(int polls, int *flag) {
     }
     __syncthreads();
     const bool done = wait_parity(smem_u32(&bar), 0u, polls);
-    if (threadIdx.x == 0) *flag = done ? 0 : 1;
+    const int code = done ? 0 : drain_after_timeout(smem_u32(&bar), 0u, polls, 4);
+    if (threadIdx.x == 0) *flag = code;
 }
 
 }  // namespace
