@@ -17,7 +17,8 @@ line on rank 0:
               over its CUDA-event time, against MEASURED_PEAKS.json
   cpu_baseline the oracle's table-driven port (OpenMP) on the host cores, on a
               bounded slice of the same workload
-  variants    recon-12, FP64 and the 3D operator on 24^3x48 (not the headline)
+  variants    recon-12, FP64, the 3D operator on 24^3x48, several right-hand
+              sides on 24^3x48, the uneven batch, the force (not the headline)
 
 --impl reference times the CPU implementation of the path on the host cores:
 the reference library built from its own sources (oracle/_ref) where it was
@@ -43,10 +44,19 @@ DIMS_3D = (24, 24, 24, 48)
 FLOPS_4D, FLOPS_3D = 1320, 984
 WORKLOAD = "wilson_dslash_4d_32x32x32x64_f32_recon18"
 METRIC = "Dslash GFLOP/s at 32^3x64 (FP32, 4D, 18-real links, 1320 flop/site)"
+DATA = "synthetic: random SU(3) links (Gaussian, Gram-Schmidt, row2 = conj(row0 x row1)), N(0,1) spinors"
 
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+def headline_config(sites):
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": WORKLOAD, "lattice": list(DIMS), "nd": 4, "prec": 32, "recon": 18,
+            "sites_per_step": sites, "flops_per_site": FLOPS_4D, "bytes_per_site": 2 * 96 + 8 * 72,
+            "l2": "no flush: inputs (gauge %d MiB, spinors 2 x %d MiB) exceed the 129 MB L2"
+                  % (2 * sites * 4 * 72 >> 20, sites * 96 >> 20)}
 
 
 def dist_env():
@@ -403,6 +413,57 @@ def uneven_batch(torch, peak):
     return out
 
 
+def force_variants(torch, peak, steps):
+    """dL/dU of L = Re <chi, D psi> for every link (gbds_op_force, mode 1: the
+    su(3) force TA(G U^+), written in the packed gauge layout), at the
+    configured sizes: 32^3x64 in FP32 and 16^4 in FP64.  Algorithmic bytes per
+    call: the V/2 source spinors and V/2 chi spinors read once, the 4 links
+    of each site read once and their forces written once: V (s + 8 g), s and
+    g the bytes of a spinor and of a link.  Each call is timed alone with CUDA
+    events, after writing a 256 MiB buffer so that no input is left in L2 (the
+    16^4 fields would fit in it)."""
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    out = {}
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    for dims, prec in (((32, 32, 32, 64), 32), ((16, 16, 16, 16), 64)):
+        dt = torch.float32 if prec == 32 else torch.float64
+        op = DslashOperator(dims, nd=4, prec=prec, recon=18)
+        V = op.volume
+        u, psi = make_fields(dims, dt, torch, seed=21)
+        gen = torch.Generator(device="cuda").manual_seed(22)
+        chi = torch.randn(V * 24, dtype=dt, device="cuda", generator=gen)
+        gauge = op.pack_gauge(u)
+        srcs = {cb: (op.pack_spinor(psi, cb), op.pack_spinor(chi, 1 - cb)) for cb in (0, 1)}
+        del u, psi, chi
+        f = torch.empty(V * 72, dtype=dt, device="cuda")
+        combos = [(1, 0), (-1, 1), (-1, 0), (1, 1)]
+        stream = torch.cuda.current_stream()
+        for k in range(3):
+            isign, cb = combos[k % 4]
+            op.force(gauge, srcs[cb][0], srcs[cb][1], isign, cb, f, mode=1, stream=stream)
+        n = max(10, min(steps, 50))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for k in range(n):
+            isign, cb = combos[k % 4]
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+            op.force(gauge, srcs[cb][0], srcs[cb][1], isign, cb, f, mode=1, stream=stream)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / n
+        real = 4 if prec == 32 else 8
+        nbytes = V * (24 * real + 8 * 18 * real)
+        gbs = nbytes / (ms * 1e6)
+        out["force_%s_f%d" % ("x".join(map(str, dims)), prec)] = {
+            "ms": ms, "gbs": gbs, "roofline_frac": gbs / peak, "bytes_per_call": nbytes,
+            "links": 4 * V, "launches_per_call": 2, "mode": "su(3) force TA(G U^+)"}
+        del gauge, srcs, f
+        op.close()
+        torch.cuda.empty_cache()
+    del flush
+    return out
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -431,25 +492,49 @@ def profiled_traffic(workload):
 # CPU legs
 # ---------------------------------------------------------------------------
 
-def cpu_port_rate(u_host, psi_host, seconds, threads=None):
-    """GFLOP/s of the oracle's table-driven port on slices of the workload."""
+def cpu_stepper(u_host, psi_host):
+    """One full application of the CPU implementation of the path on the
+    host cores, as step(k) cycling isign/cb: the reference library built from
+    its own sources (oracle/_ref) where it exists for this host, else the
+    oracle's table-driven port of it.  Returns (step, kind, threads, what)."""
     import numpy as np
     import oracle as O
-    lol = O.layout_table(O.LAYOUT_CB2, DIMS)
-    tabs = O.PortTables(4, DIMS, lol)
-    n = O.max_threads() if threads is None else threads
-    Vh = O.volume(DIMS) // 2
     res = np.zeros_like(psi_host)
-    count = max(4096, Vh // 32)
-    tabs.apply_range(u_host, psi_host, res, 1, 0, 0, count, n)  # warm-up
-    done, first, t0 = 0, 0, time.perf_counter()
+    combos = [(1, 0), (-1, 1), (-1, 0), (1, 1)]
+    threads = O.max_threads()
+    if O.reference_available(32):
+        try:
+            ref = O.Reference(32)
+            ref.init(4, DIMS, O.LAYOUT_CB2)
+
+            def step(k):
+                isign, cb = combos[k % 4]
+                ref.apply(4, u_host, psi_host, res, isign, cb)
+            return step, "reference", threads, ("sse_su3dslash_wilson of the reference library built from its own "
+                                                 "sources (OpenMP dispatch)")
+        except OSError:
+            pass
+    tabs = O.PortTables(4, DIMS, O.layout_table(O.LAYOUT_CB2, DIMS))
+
+    def step(k):
+        isign, cb = combos[k % 4]
+        tabs.apply(u_host, psi_host, res, isign, cb, threads)
+    return step, "port", threads, ("the oracle's table-driven port of the reference scalar library (OpenMP); "
+                                   "the reference sources are not on this host")
+
+
+def cpu_rate(u_host, psi_host, seconds):
+    """GFLOP/s of full applications of the CPU implementation for about
+    ``seconds`` (after one untimed application)."""
+    step, kind, threads, what = cpu_stepper(u_host, psi_host)
+    Vh = u_host.shape[0] // 2
+    step(0)
+    apps, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
-        tabs.apply_range(u_host, psi_host, res, 1, 0, first, count, n)
-        done += count
-        first = (first + count) % Vh
+        step(apps + 1)
+        apps += 1
     dt = time.perf_counter() - t0
-    tabs.close()
-    return FLOPS_4D * done / dt / 1e9, n, done, dt
+    return FLOPS_4D * Vh * apps / dt / 1e9, kind, threads, apps, dt, what
 
 
 def run_reference(args):
@@ -465,50 +550,19 @@ def run_reference(args):
     log("reference arm: generating inputs")
     u = O.random_gauge(rng, V).astype(np.float32)
     psi = O.gaussian_spinor(rng, V).astype(np.float32)
-    res = np.zeros_like(psi)
-    kind = "port"
-    ref = None
-    if O.reference_available(32):
-        try:
-            ref = O.Reference(32)
-            ref.init(4, DIMS, O.LAYOUT_CB2)
-            kind = "reference"
-        except OSError:
-            ref = None
-    threads = O.max_threads()
-    if ref is not None:
-        # one full application per step (the reference has no sub-range entry)
-        def step(k):
-            ref.apply(4, u, psi, res, 1 if k % 2 == 0 else -1, k % 2)
-        count = Vh
-        sample = "full 32^3x64 FP32 applications through sse_su3dslash_wilson (reference built from its sources)"
-    else:
-        lol = O.layout_table(O.LAYOUT_CB2, DIMS)
-        tabs = O.PortTables(4, DIMS, lol)
-        t0 = time.perf_counter()
-        tabs.apply_range(u, psi, res, 1, 0, 0, Vh // 16, threads)
-        per_site = (time.perf_counter() - t0) / (Vh // 16)
-        budget = 60.0
-        count = int(min(Vh, max(4096, budget / max(1, args.steps + args.warmup) / per_site)))
-        state = {"first": 0}
-
-        def step(k):
-            tabs.apply_range(u, psi, res, 1 if k % 2 == 0 else -1, k % 2, state["first"], count, threads)
-            state["first"] = (state["first"] + count) % Vh
-        sample = f"{count} of {Vh} target sites per step (a slice of one 32^3x64 FP32 application), oracle port"
+    step, kind, threads, what = cpu_stepper(u, psi)
+    sample = f"full {'x'.join(map(str, DIMS))} FP32 applications, isign/cb cycled: " + what
     for k in range(args.warmup):
         step(k)
     t0 = time.perf_counter()
     for k in range(args.steps):
         step(k)
     dt = time.perf_counter() - t0
-    value = FLOPS_4D * count * args.steps / dt / 1e9
+    value = FLOPS_4D * Vh * args.steps / dt / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: random SU(3) links (Gram-Schmidt), N(0,1) spinors",
-            "config": {"workload": WORKLOAD, "lattice": list(DIMS), "nd": 4, "prec": 32, "recon": 18,
-                       "sites_per_step": count, "flops_per_site": FLOPS_4D},
+            "data": DATA, "config": headline_config(Vh),
             "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -654,10 +708,10 @@ def run_gb300(args):
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             uh = u_h.numpy().reshape(-1, 4, 3, 3, 2)
             ph = psi_h.numpy().reshape(-1, 4, 3, 2)
-            rate, n, done, secs = cpu_port_rate(uh, ph, args.cpu_seconds)
-            cpu = {"value": rate, "unit": "GFLOP/s", "cores": n, "kind": "port",
-                   "sample": f"{done} target sites ({done / sites:.2f} applications) of {'x'.join(map(str, DIMS))} FP32, "
-                             f"isign=+1 cb=0, oracle table-driven port, {secs:.1f} s"}
+            rate, kind, n, apps, secs, what = cpu_rate(uh, ph, args.cpu_seconds)
+            cpu = {"value": rate, "unit": "GFLOP/s", "cores": n, "kind": kind,
+                   "sample": f"{apps} full {'x'.join(map(str, DIMS))} FP32 applications in {secs:.1f} s, isign/cb "
+                             f"cycled, on the same inputs as the GPU: " + what}
         del u_h, psi_h, res_h
 
     # -- variants (not the headline) -------------------------------------------
@@ -688,6 +742,8 @@ def run_gb300(args):
             torch.cuda.empty_cache()
         if run("uneven_batch"):
             variants["uneven_batch"] = uneven_batch(torch, peak)
+        if run("force"):
+            variants.update(force_variants(torch, peak, vsteps))
 
     solver = None
     if not args.no_solver:
@@ -697,13 +753,9 @@ def run_gb300(args):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic: random SU(3) links (Gaussian, Gram-Schmidt, row2 = conj(row0 x row1)), N(0,1) spinors",
-                "config": {"workload": WORKLOAD, "lattice": list(DIMS), "nd": 4, "prec": 32, "recon": 18,
-                           "sites_per_step": sites, "flops_per_site": FLOPS_4D, "bytes_per_site": bytes_per_site,
-                           "l2": "no flush: inputs (gauge 576 MiB, spinors 2 x 96 MiB) exceed the 129 MB L2",
-                           "parallelism": "replicas" if world > 1 else "single GPU",
-                           "tuning": {"block": tuning[0], "variant": tuning[1]}},
+                "vs_baseline": None, "dtype": "f32", "data": DATA, "config": headline_config(sites),
+                "parallelism": "replicas" if world > 1 else "single GPU",
+                "tuning": {"block": tuning[0], "variant": tuning[1]},
                 "hbm_gbs": achieved,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_source": peak_kind,
@@ -731,7 +783,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true")
     ap.add_argument("--variants", default="all",
-                    help="comma list of variant sections: recon12, f64, 3d, multi_rhs, uneven_batch (default all)")
+                    help="comma list of variant sections: recon12, f64, 3d, multi_rhs, uneven_batch, force (default all)")
     ap.add_argument("--tuning", default=None,
                     help="block,variant of the headline kernel instead of autotuning (for profiling runs)")
     ap.add_argument("--dims", default=None,

@@ -211,7 +211,8 @@ long long gbds_kernel_launch_count(void);
  *   call is made.
  *   The first call on each device looks up that device's address of the
  *   array (cudaGetSymbolAddress) with the device current; make that first call
- *   before any stream capture.
+ *   before any stream capture.  The address is kept for the life of the
+ *   process, so a cudaDeviceReset between calls is not supported.
  *   All calls share the array and it keeps the last call's contents (every
  *   element a call reads it has written first).  Calls that overlap on the
  *   GPU -- different streams, or different host threads -- race on it: issue

@@ -73,11 +73,13 @@ def _unpack_complex(f):
     return O.unpack_links(f.reshape(-1, 4, 3, 3, 2))  # [V,4,i,j]
 
 
+@pytest.mark.parametrize("dims", [(4, 4, 2, 4), (16, 16, 16, 16)])
 @pytest.mark.parametrize("isign,cb", [(1, 0), (-1, 1)])
-def test_gradient_matches_numpy(isign, cb):
+def test_gradient_matches_numpy(isign, cb, dims):
+    """The complex gradient dL/dU of every link (mode 0) against the FP64
+    numpy gradient; 16^4 is the configured FP64 size."""
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
-    dims = (4, 4, 2, 4)
     rng = np.random.default_rng(5)
     V = O.volume(dims)
     u = O.random_gauge(rng, V)
@@ -108,10 +110,13 @@ def _force(dims, prec, u, psi, chi, isign, cb):
     return _unpack_complex(out.double().cpu().numpy()).reshape(-1, 3, 3)
 
 
+@pytest.mark.parametrize("dims", [(4, 4, 4, 4), (16, 16, 16, 16)])
 @pytest.mark.parametrize("isign,cb", [(1, 0), (-1, 1)])
-def test_force_matches_finite_differences(isign, cb):
+def test_force_matches_finite_differences(isign, cb, dims):
+    """The su(3) force (mode 1) against FP64 central differences of L along a
+    random su(3) direction on every link (step 1e-6); 16^4 is the configured
+    FP64 size."""
     from sse_wilson_dslash_gb300.device import DslashOperator
-    dims = (4, 4, 4, 4)
     rng = np.random.default_rng(6)
     V = O.volume(dims)
     u = O.random_gauge(rng, V)
@@ -149,13 +154,13 @@ def test_dL_dpsi_is_dslash_dagger():
     assert abs(pred - fd) <= 1e-8 * abs(fd)
 
 
-def test_solver_force_matches_finite_differences():
+@pytest.mark.parametrize("dims", [(4, 4, 4, 4), (16, 16, 16, 16)])
+def test_solver_force_matches_finite_differences(dims):
     """S = phi^+ (M^+M)^-1 phi, M = 1 - kappa^2 D_eo D_oe:
     dS = 2 kappa^2 (Re<Y, dD_eo Z> + Re<W, dD_oe X>), X = (M^+M)^-1 phi,
-    Y = M X, Z = D_oe X, W = D_eo^+ Y."""
+    Y = M X, Z = D_oe X, W = D_eo^+ Y.  16^4 is the configured FP64 size."""
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator, WilsonSolver
-    dims = (4, 4, 4, 4)
     kappa = 0.124
     rng = np.random.default_rng(9)
     V = O.volume(dims)
@@ -213,3 +218,38 @@ def test_autograd_gradcheck():
     for isign, cb in ((1, 0), (-1, 1)):
         assert torch.autograd.gradcheck(lambda a, b: DslashFn.apply(a, b, op, isign, cb), (u, psi),
                                         eps=1e-6, atol=1e-8, rtol=1e-6)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("isign,cb", [(1, 0), (-1, 1)])
+def test_fp32_force_32x32x32x64_matches_fp64(isign, cb):
+    """At the configured FP32 size, 32^3x64, the FP32 su(3) force of every link
+    against the FP64 force of the same inputs: the largest per-link
+    difference is at most 2e-6 of the largest per-link force, and the
+    difference over all links at most 1e-6 of the force (Frobenius norms;
+    FP32 rounding of the inputs and of the arithmetic, unit 6e-8)."""
+    import torch
+    from bench import su3_links
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims = (32, 32, 32, 64)
+    V = O.volume(dims)
+    gen = torch.Generator(device="cuda").manual_seed(12)
+    u = su3_links(V * 4, gen, torch).reshape(-1)
+    psi = torch.randn(V * 24, dtype=torch.float64, device="cuda", generator=gen)
+    chi = torch.randn(V * 24, dtype=torch.float64, device="cuda", generator=gen)
+    forces = {}
+    for prec, dt in ((64, torch.float64), (32, torch.float32)):
+        op = DslashOperator(dims, prec=prec)
+        gauge = op.pack_gauge(u.to(dt))
+        ps = op.pack_spinor(psi.to(dt), cb)
+        cs = op.pack_spinor(chi.to(dt), 1 - cb)
+        out = torch.zeros(V * 72, dtype=dt, device="cuda")
+        op.force(gauge, ps, cs, isign, cb, out, mode=1)
+        torch.cuda.synchronize()
+        forces[prec] = out.double().view(V * 4, 18)
+        del gauge, ps, cs
+        op.close()
+    d = (forces[32] - forces[64]).norm(dim=1)
+    f = forces[64].norm(dim=1)
+    assert d.max().item() <= 2e-6 * f.max().item(), (d.max().item(), f.max().item())
+    assert d.norm().item() <= 1e-6 * f.norm().item()

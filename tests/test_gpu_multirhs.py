@@ -4,26 +4,12 @@ import numpy as np
 import pytest
 
 import oracle as O
+from formats import TOL, TOL_TC, site_err, stored
 
 pytestmark = pytest.mark.gpu
 
-# Per-site tolerances: FP32 as the parity tests; bfloat16 storage rounds
-# inputs and outputs to 8 significant bits (2^-9 relative per component);
-# half + norm to 11 bits of the site's largest component.
-TOL = {"native": 1e-6, "f32_pairs": 1e-6, "bf16": 1.2e-2, "f16": 3e-3}
-
-
 def _round(psi, fmt):
-    import torch
-    t = torch.from_numpy(psi.astype(np.float32))
-    if fmt == "bf16":
-        return t.to(torch.bfloat16).float().numpy().astype(np.float64)
-    if fmt == "f16":
-        v = t.reshape(-1, 24)
-        m = v.abs().amax(1, keepdim=True)
-        q = (v / torch.where(m > 0, m, torch.ones_like(m))).half().float() * m
-        return q.reshape(t.shape).numpy().astype(np.float64)
-    return psi.astype(np.float32).astype(np.float64)
+    return stored(psi, fmt)
 
 
 @pytest.mark.parametrize("fmt", ["native", "f32_pairs", "bf16", "f16"])
@@ -132,7 +118,7 @@ def test_tensor_core_multi_rhs_matches_oracle(nrhs, fmt, dims):
             for r in range(nrhs):
                 ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
                 err = O.site_rel_err(got[r], ref, ts)
-                assert err <= TOL[fmt], (recon, isign, cb, r, err)
+                assert err <= TOL_TC[fmt], (recon, isign, cb, r, err)
         op.close()
 
 
@@ -171,7 +157,7 @@ def test_autotune_chooses_between_cuda_and_tensor_cores(fmt):
     ts = O.target_sites(4, dims, lol, 0)
     for r in range(0, nrhs, 7):
         ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), 1, 0)
-        assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt]
+        assert O.site_rel_err(got[r], ref, ts) <= TOL_TC.get(fmt, TOL[fmt])
     op.close()
 
 
@@ -203,7 +189,7 @@ def test_tensor_core_edge_lattices(dims, nrhs):
         ts = O.target_sites(4, dims, lol, cb)
         for r in range(nrhs):
             ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
-            assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt], (dims, isign, cb, r)
+            assert O.site_rel_err(got[r], ref, ts) <= TOL_TC[fmt], (dims, isign, cb, r)
     op.close()
 
 
@@ -216,40 +202,76 @@ def test_tensor_core_wait_times_out_and_reports():
     test_tensor_core_edge_lattices((2, 4, 6, 2), 32)
 
 
-@pytest.mark.slow
-def test_tensor_core_production_lattice():
-    """24^3x48, 32 rhs, BF16: the tensor-core and CUDA-core kernels agree
-    site by site for every rhs (both within the BF16 bound of the oracle),
-    and three rhs are checked against the oracle directly."""
+# ---------------------------------------------------------------------------
+# The configured size: 24^3x48, one random SU(3) field, up to 32 rhs
+# ---------------------------------------------------------------------------
+
+PROD_DIMS = (24, 24, 24, 48)
+PROD_ISIGN, PROD_CB = -1, 0
+
+
+@pytest.fixture(scope="module")
+def production():
+    """Inputs at 24^3x48 and the oracle's outputs for all 32 rhs, per stored
+    format (FP32, bfloat16, half + norm), on the target sites, on the device."""
+    import torch
+    from bench import su3_links
+    dims, nrhs = PROD_DIMS, 32
+    V = O.volume(dims)
+    gen = torch.Generator(device="cuda").manual_seed(2024)
+    u = su3_links(V * 4, gen, torch).float().reshape(-1)
+    psi = torch.randn(nrhs, V * 24, dtype=torch.float32, device="cuda", generator=gen)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    ts = O.target_sites(4, dims, lol, PROD_CB)
+    uh, ph = u.cpu().numpy(), psi.cpu().numpy()
+    refs = {}
+    for kind in ("native", "bf16", "f16"):
+        src = stored(ph, kind)
+        refs[kind] = torch.from_numpy(np.stack([
+            O.dslash_plain(4, dims, lol, uh, src[r], PROD_ISIGN, PROD_CB).reshape(V, 24)[ts]
+            for r in range(nrhs)])).cuda()
+    return dict(u=u, psi=psi, refs=refs, ts=torch.from_numpy(ts).cuda(), V=V)
+
+
+def _production_error(production, nrhs, fmt, variant=None, tc=False):
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
-    dims, nrhs, fmt = (24, 24, 24, 48), 32, "bf16"
-    V = O.volume(dims)
-    lol = O.layout_table(O.LAYOUT_CB2, dims)
-    rng = np.random.default_rng(2024)
-    u = O.random_gauge(rng, V).astype(np.float32)
-    g = torch.Generator(device="cuda").manual_seed(11)
-    psi = torch.randn(nrhs * V * 24, dtype=torch.float32, device="cuda", generator=g)
-    outs = {}
-    for tc in (False, True):
-        op = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
-        op.set_tensor_cores(tc)
-        gauge = op.pack_gauge(torch.from_numpy(u.ravel()).cuda())
-        out = op.apply(gauge, op.pack_spinor(psi, 0), -1, 0)
-        op.check()
-        res = torch.zeros(nrhs * V * 24, dtype=torch.float32, device="cuda")
-        op.unpack_spinor(out, 1, res)
-        outs[tc] = res.view(nrhs, V, 24)
-        op.close()
-    ts = torch.from_numpy(O.target_sites(4, dims, lol, 0)).cuda()
-    a, b = outs[True][:, ts].double(), outs[False][:, ts].double()
-    rel = ((a - b).norm(dim=2) / b.norm(dim=2)).max().item()
-    assert rel <= 2 * TOL[fmt], rel
-    for r in (0, 13, 31):
-        p = psi.view(nrhs, V * 24)[r].cpu().numpy().astype(np.float64)
-        ref = O.dslash_plain(4, dims, lol, u, _round(p, fmt), -1, 0)
-        got = outs[True][r].cpu().numpy()
-        assert O.site_rel_err(got, ref, O.target_sites(4, dims, lol, 0)) <= TOL[fmt], r
+    P = production
+    op = DslashOperator(PROD_DIMS, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
+    if tc:
+        op.set_tensor_cores(True)
+    elif variant is not None:
+        op.set_tuning(0, variant)
+    gauge = op.pack_gauge(P["u"])
+    out = op.apply(gauge, op.pack_spinor(P["psi"][:nrhs].reshape(-1), PROD_CB), PROD_ISIGN, PROD_CB)
+    op.check()
+    res = torch.zeros(nrhs * P["V"] * 24, dtype=torch.float32, device="cuda")
+    op.unpack_spinor(out, 1 - PROD_CB, res)
+    got = res.view(nrhs, P["V"], 24)[:, P["ts"]].double()
+    ref = P["refs"]["native" if fmt == "f32_pairs" else fmt][:nrhs]
+    op.close()
+    return ((got - ref).norm(dim=2) / ref.norm(dim=2)).max().item()
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("fmt,variants", [("native", (0, 1)), ("f32_pairs", (1, 2)), ("bf16", (0, 2)),
+                                          ("f16", (2,))])
+@pytest.mark.parametrize("nrhs", [16, 32])
+def test_multi_rhs_24x24x24x48_every_rhs_against_oracle(production, nrhs, fmt, variants):
+    """Every rhs and target site at the configured size, for the CUDA-core
+    variants the autotuner chooses among (0 plain, 1 packed colour multiply,
+    2 fully packed), within the storage format's bound."""
+    for v in variants:
+        err = _production_error(production, nrhs, fmt, variant=v)
+        assert err <= TOL[fmt], (nrhs, fmt, v, err)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("fmt", ["bf16", "f16"])
+@pytest.mark.parametrize("nrhs", [16, 32])
+def test_tensor_core_24x24x24x48_every_rhs_against_oracle(production, nrhs, fmt):
+    err = _production_error(production, nrhs, fmt, tc=True)
+    assert err <= TOL_TC[fmt], (nrhs, fmt, err)
 
 
 @pytest.mark.parametrize("fmt", ["native", "f32_pairs", "bf16", "f16"])

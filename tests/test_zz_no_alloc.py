@@ -6,12 +6,15 @@ device array, so it takes lattices of at most 32768 sites.
 
 Checked through the C ABI against the allocating operator-handle path
 (gbds_op_pack_* + gbds_op_dslash + gbds_op_unpack_spinor) on the same inputs,
-on two calls in a row, with the per-site tolerance of the FP32 parity tests.
-This file is collected last."""
+on two calls in a row, and against the CPU oracle, with the per-site
+tolerance of the FP32 parity tests; the device's free memory is the same
+before and after a call.  This file is collected last."""
 import ctypes
 
 import numpy as np
 import pytest
+
+import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -97,3 +100,43 @@ def test_noalloc_rejects_lattices_above_the_limit(lib):
                                             ctypes.c_void_p(u.data_ptr()), 1, 0, None)
     assert rc == 1
     assert b"no-allocation limit of 32768 sites" in lib.gbds_get_last_error()
+
+
+@pytest.mark.parametrize("nd,dims", [(4, (8, 8, 4, 8)), (3, (4, 6, 4, 5))])
+def test_noalloc_matches_oracle(lib, nd, dims):
+    """Seeded random SU(3) links and N(0,1) spinors in the QDP++ order (cb2 for
+    4D, cb3d for 3D), every target site against the oracle, all four isign /
+    cb combinations."""
+    import torch
+    V = int(np.prod(dims))
+    lol = O.layout_table(O.LAYOUT_CB2 if nd == 4 else O.LAYOUT_CB3D, dims)
+    u, psi = O.make_inputs(dims, 101, 102)
+    u, psi = u.astype(np.float32), psi.astype(np.float32)
+    ud = torch.from_numpy(u.ravel()).cuda()
+    pd = torch.from_numpy(psi.ravel()).cuda()
+    for isign, cb in ((1, 0), (1, 1), (-1, 0), (-1, 1)):
+        got = _noalloc(lib, dims, nd, ud, pd, isign, cb, torch).cpu().numpy()
+        ref = O.dslash_plain(nd, dims, lol, u, psi, isign, cb)
+        assert O.site_rel_err(got, ref, O.target_sites(nd, dims, lol, cb)) <= FP32_SITE_TOL, (isign, cb)
+
+
+def test_noalloc_leaves_device_free_memory_unchanged(lib):
+    """After a first call (which may load the library's device code and with
+    it the static array), a further call changes the device's free memory by
+    nothing: it allocates no device memory."""
+    import torch
+    dims = (8, 8, 8, 16)
+    V = int(np.prod(dims))
+    u, psi = _fields(torch, V, 7)
+    out = torch.zeros(V * 24, dtype=torch.float32, device="cuda")
+    d = (ctypes.c_int * 4)(*dims)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    args = (d, 4, ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(out.data_ptr()))
+    assert lib.gbds_dslash_packed_noalloc_f32(*args, 1, 0, s) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for isign, cb in ((-1, 1), (1, 0)):
+        assert lib.gbds_dslash_packed_noalloc_f32(*args, isign, cb, s) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
