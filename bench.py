@@ -771,6 +771,61 @@ def run_gb300(args):
     return 0
 
 
+def run_profile_case(args):
+    """--profile KIND: build one operator on --dims and launch only its kernel,
+    --warmup + --steps times, for an ncu capture (-k, -s, -c select the
+    launches).  KIND: dslash (--prec, --recon), force (--prec; the su(3)
+    force), multi_rhs (--nrhs, --fmt, --variant or --tc).  Prints one JSON
+    line with the mean CUDA-event time of the timed launches; nothing else is
+    allocated beyond the operator's fields."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims = DIMS
+    V = dims[0] * dims[1] * dims[2] * dims[3]
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    kind = args.profile
+    if kind == "multi_rhs":
+        op = DslashOperator(dims, nd=4, prec=32, recon=args.recon, nrhs=args.nrhs, spinor_format=args.fmt)
+        if args.tc:
+            op.set_tensor_cores(True)
+        elif args.variant >= 0:
+            op.set_tuning(0, args.variant)
+        u = su3_links(V * 4, gen, torch).float().reshape(-1)
+        psi = torch.randn(args.nrhs * V * 24, dtype=torch.float32, device="cuda", generator=gen)
+    else:
+        dt = torch.float32 if args.prec == 32 else torch.float64
+        op = DslashOperator(dims, nd=4, prec=args.prec, recon=args.recon if kind == "dslash" else 18)
+        if kind == "dslash" and args.variant >= 0:
+            op.set_tuning(0, args.variant)
+        u = su3_links(V * 4, gen, torch).to(dt).reshape(-1)
+        psi = torch.randn(V * 24, dtype=dt, device="cuda", generator=gen)
+    gauge = op.pack_gauge(u)
+    src = op.pack_spinor(psi, 0)
+    if kind == "force":
+        chi = op.pack_spinor(psi, 1)
+        f = torch.empty_like(u)
+        launch = lambda: op.force(gauge, src, chi, 1, 0, f, mode=1)  # noqa: E731
+    else:
+        res = op.new_spinor()
+        launch = lambda: op.apply(gauge, src, 1, 0, out=res)  # noqa: E731
+    del u, psi
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        launch()
+    e1.record()
+    torch.cuda.synchronize()
+    op.check()
+    print(json.dumps({"profile": kind, "dims": list(dims), "ms": e0.elapsed_time(e1) / args.steps,
+                      "tuning": list(op.tuning())}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -788,6 +843,14 @@ def main():
                     help="block,variant of the headline kernel instead of autotuning (for profiling runs)")
     ap.add_argument("--dims", default=None,
                     help="Lx,Ly,Lz,Lt of the 4D workload (default 32,32,32,64; smaller cases are for profiling)")
+    ap.add_argument("--profile", choices=["dslash", "force", "multi_rhs"], default=None,
+                    help="build one operator on --dims and launch only its kernel (for ncu captures)")
+    ap.add_argument("--prec", type=int, default=32, help="--profile dslash/force: 32 or 64")
+    ap.add_argument("--recon", type=int, default=18, help="--profile dslash/multi_rhs: 18 or 12")
+    ap.add_argument("--nrhs", type=int, default=32, help="--profile multi_rhs: right-hand sides")
+    ap.add_argument("--fmt", default="bf16", help="--profile multi_rhs: native, f32_pairs, bf16 or f16")
+    ap.add_argument("--variant", type=int, default=-1, help="--profile: kernel variant (-1: the default)")
+    ap.add_argument("--tc", action="store_true", help="--profile multi_rhs: the tensor-core kernel")
     args = ap.parse_args()
     if args.dims:
         global DIMS, WORKLOAD
@@ -795,6 +858,8 @@ def main():
         WORKLOAD = "wilson_dslash_4d_%dx%dx%dx%d_f32_recon18" % DIMS
     if args.warmup < 3:
         args.warmup = 3
+    if args.profile:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

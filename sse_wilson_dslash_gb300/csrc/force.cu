@@ -17,6 +17,8 @@
 // operator.  Output: the packed gauge layout, f[s][mu][j][i] = F_ij.
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include "dslash_kernel.cuh"
 
 namespace gbds {
@@ -98,12 +100,18 @@ struct ForceArgs {
     int accumulate;
 };
 
+// Sites per CTA: 128 in FP32, 64 in FP64, so that the staged output of a CTA
+// (4 links x 18 reals per site) is 36 KB of shared memory either way.
+template <typename T> struct ForceTile { static constexpr int sites = sizeof(T) == 4 ? 128 : 64; };
+
+// R = G (mode 0) or TA(G U^+) (mode 1) of link (p, h, MU), times coef, into
+// the CTA's staging area at the site's slot: stage[slot*72 + MU*18 + (3j+i)*2]
+// holds R_ij, the packed transposed order of the output.
 template <typename T, int ISIGN, int MU>
-__device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, const Nbr &n) {
+__device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, const Nbr &n, const cx<T> (&own)[4][3],
+                                           T *stage) {
     using F = Field<T>;
     using V = typename VecOf<T>::S;
-    const V *psi = static_cast<const V *>(a.psi);
-    const V *chi = static_cast<const V *>(a.chi);
     cx<T> G[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -111,18 +119,16 @@ __device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, con
         for (int j = 0; j < 3; j++) G[i][j] = {T(0), T(0)};
     cx<T> s[4][3], hs[2][3], xi[2][3];
     if (p == a.pt) {
-        // forward hop at x: xi from chi(x), half spinor of psi(x + mu)
-        F::load_spinor(chi, a.g.stride, h, s);
-        fold<MU, ISIGN>(s, xi);
-        F::load_spinor(psi, a.g.stride, n.f[MU], s);
+        // forward hop at x: xi from chi(x) (own), half spinor of psi(x + mu)
+        fold<MU, ISIGN>(own, xi);
+        F::load_spinor(static_cast<const V *>(a.psi), a.g.stride, n.f[MU], s);
         project<MU, ISIGN>(s, hs);
         outer_acc(G, xi[0], hs[0]);
         outer_acc(G, xi[1], hs[1]);
     } else {
-        // backward hop into y = x + mu: half spinor of psi(x), xi from chi(y)
-        F::load_spinor(psi, a.g.stride, h, s);
-        project<MU, -ISIGN>(s, hs);
-        F::load_spinor(chi, a.g.stride, n.f[MU], s);
+        // backward hop into y = x + mu: half spinor of psi(x) (own), xi from chi(y)
+        project<MU, -ISIGN>(own, hs);
+        F::load_spinor(static_cast<const V *>(a.chi), a.g.stride, n.f[MU], s);
         fold<MU, -ISIGN>(s, xi);
         outer_acc(G, hs[0], xi[0]);
         outer_acc(G, hs[1], xi[1]);
@@ -138,36 +144,76 @@ __device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, con
 #pragma unroll
             for (int j = 0; j < 3; j++) R[i][j] = G[i][j];
     }
-    const int i_int = p * a.g.Vh + h;
-    const int site = a.table ? a.table[i_int] : i_int;
-    T *o = static_cast<T *>(a.out) + ((size_t)site * 4 + MU) * 18;
     const T c = (T)a.coef;
+    T *o = stage + MU * 18;
 #pragma unroll
     for (int j = 0; j < 3; j++)
 #pragma unroll
-        for (int i = 0; i < 3; i++) {  // packed transposed: o[j][i] = R_ij
-            T *d = o + (j * 3 + i) * 2;
-            if (a.accumulate) {
-                d[0] += c * R[i][j].r;
-                d[1] += c * R[i][j].i;
-            } else {
-                d[0] = c * R[i][j].r;
-                d[1] = c * R[i][j].i;
-            }
+        for (int i = 0; i < 3; i++) {
+            o[(j * 3 + i) * 2] = c * R[i][j].r;
+            o[(j * 3 + i) * 2 + 1] = c * R[i][j].i;
         }
 }
 
-// One thread per site of checkerboard p; all four links of the site.
+// One thread per site of checkerboard p = blockIdx.y (both checkerboards in
+// one launch; they own disjoint links), all four links of the site.  The
+// site's own spinor (chi on checkerboard pt, psi on cb) is loaded once for
+// the four links.  The results are staged in shared memory and written with
+// 16-byte stores: in the canonical layout a CTA's sites are one contiguous
+// run of the packed output, which its threads write in order; with a caller
+// layout each warp writes its sites' 72-real blocks one site at a time.
 template <typename T, int ISIGN>
-__global__ void __launch_bounds__(128) force_kernel(const ForceArgs a, int p) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= a.g.Vh) return;
-    Nbr n;
-    neighbours<4>(a.g, h, p, n);
-    force_link<T, ISIGN, 0>(a, p, h, n);
-    force_link<T, ISIGN, 1>(a, p, h, n);
-    force_link<T, ISIGN, 2>(a, p, h, n);
-    force_link<T, ISIGN, 3>(a, p, h, n);
+__global__ void __launch_bounds__(ForceTile<T>::sites) force_kernel(const ForceArgs a) {
+    using F = Field<T>;
+    using V = typename VecOf<T>::S;
+    using Q = typename VecOf<T>::S;  // 16-byte vector: float4 or double2
+    constexpr int NS = ForceTile<T>::sites;
+    constexpr int QPS = 72 * (int)sizeof(T) / 16;  // 16-byte vectors per site
+    __shared__ __align__(16) T stage[NS * 72];
+    const int p = blockIdx.y;
+    const int h0 = blockIdx.x * NS;
+    const int h = h0 + threadIdx.x;
+    if (h < a.g.Vh) {
+        Nbr n;
+        neighbours<4>(a.g, h, p, n);
+        cx<T> own[4][3];
+        F::load_spinor(static_cast<const V *>(p == a.pt ? a.chi : a.psi), a.g.stride, h, own);
+        T *st = stage + threadIdx.x * 72;
+        force_link<T, ISIGN, 0>(a, p, h, n, own, st);
+        force_link<T, ISIGN, 1>(a, p, h, n, own, st);
+        force_link<T, ISIGN, 2>(a, p, h, n, own, st);
+        force_link<T, ISIGN, 3>(a, p, h, n, own, st);
+    }
+    __syncthreads();
+    const int nsites = min(NS, a.g.Vh - h0);
+    const Q *sq = reinterpret_cast<const Q *>(stage);
+    Q *out = static_cast<Q *>(a.out);
+    if (!a.table) {
+        Q *dst = out + (size_t)(p * a.g.Vh + h0) * QPS;
+        for (int i = threadIdx.x; i < nsites * QPS; i += NS) {
+            Q v = sq[i];
+            if (a.accumulate) {
+                const Q w = dst[i];
+                if constexpr (sizeof(T) == 4) v = make_float4(w.x + v.x, w.y + v.y, w.z + v.z, w.w + v.w);
+                else v = make_double2(w.x + v.x, w.y + v.y);
+            }
+            dst[i] = v;
+        }
+    } else {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int k = w * 32; k < min(nsites, w * 32 + 32); k++) {
+            Q *dst = out + (size_t)a.table[p * a.g.Vh + h0 + k] * QPS;
+            for (int i = lane; i < QPS; i += 32) {
+                Q v = sq[k * QPS + i];
+                if (a.accumulate) {
+                    const Q w2 = dst[i];
+                    if constexpr (sizeof(T) == 4) v = make_float4(w2.x + v.x, w2.y + v.y, w2.z + v.z, w2.w + v.w);
+                    else v = make_double2(w2.x + v.x, w2.y + v.y);
+                }
+                dst[i] = v;
+            }
+        }
+    }
 }
 
 }  // namespace
@@ -196,18 +242,21 @@ extern "C" int gbds_op_force(gbds_op op, const void *gauge, const void *psi, con
     a.mode = mode;
     a.coef = coef;
     a.accumulate = accumulate ? 1 : 0;
+    if ((reinterpret_cast<uintptr_t>(force_packed) & 15u) != 0)
+        return set_error(GBDS_ERROR_INVALID_VALUE, "force_packed must be 16-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const dim3 grid((op->g.Vh + 127) / 128);
-    for (int p = 0; p < 2; p++) {
-        if (op->prec == 32) {
-            if (isign > 0) force_kernel<float, 1><<<grid, 128, 0, st>>>(a, p);
-            else force_kernel<float, -1><<<grid, 128, 0, st>>>(a, p);
-        } else {
-            if (isign > 0) force_kernel<double, 1><<<grid, 128, 0, st>>>(a, p);
-            else force_kernel<double, -1><<<grid, 128, 0, st>>>(a, p);
-        }
-        count_launch();
+    if (op->prec == 32) {
+        constexpr int ns = ForceTile<float>::sites;
+        const dim3 grid((op->g.Vh + ns - 1) / ns, 2);
+        if (isign > 0) force_kernel<float, 1><<<grid, ns, 0, st>>>(a);
+        else force_kernel<float, -1><<<grid, ns, 0, st>>>(a);
+    } else {
+        constexpr int ns = ForceTile<double>::sites;
+        const dim3 grid((op->g.Vh + ns - 1) / ns, 2);
+        if (isign > 0) force_kernel<double, 1><<<grid, ns, 0, st>>>(a);
+        else force_kernel<double, -1><<<grid, ns, 0, st>>>(a);
     }
+    count_launch();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "gbds_op_force");
 }
