@@ -14,8 +14,8 @@ Contents
 * three restatements of the operator (``dslash_plain`` and ``PortTables`` from
   ``dslash_oracle.c``; ``dslash_numpy`` vectorised in numpy);
 * a loader for the reference library compiled from its own sources by
-  ``oracle/Makefile`` into ``oracle/_ref`` (only where the sources exist and
-  the host is x86_64).
+  ``oracle/Makefile`` into ``oracle/_ref`` (where the sources exist; with the
+  host's SSE on x86_64, else through the portable shim ``sse_shim/``).
 
 Packed layouts (the reference ABI):
   spinor ``psi[V][4 spin][3 colour][2]`` in the caller's linear site order;
@@ -356,18 +356,25 @@ def target_sites(nd: int, dims, lin_of_lex: np.ndarray, cb: int) -> np.ndarray:
 
 
 # --------------------------------------------------------------------------
-# The reference library built from its own sources (x86_64 only)
+# The reference library built from its own sources
 # --------------------------------------------------------------------------
 
-def reference_available(prec: int) -> bool:
-    return os.path.exists(os.path.join(HERE, "_ref", f"libref{prec}.so"))
+def _ref_path(prec: int, shim: bool) -> str:
+    return os.path.join(HERE, "_ref", f"libref{prec}{'_shim' if shim else ''}.so")
+
+
+def reference_available(prec: int, shim: bool = False) -> bool:
+    """The reference library built from its sources: ``shim=False`` the build
+    for this host (native SSE on x86_64, the portable SSE shim elsewhere),
+    ``shim=True`` the shim build made beside the native one on x86_64."""
+    return os.path.exists(_ref_path(prec, shim))
 
 
 class Reference:
     """ctypes binding of the reference scalar library (``oracle/_ref``)."""
 
-    def __init__(self, prec: int):
-        path = os.path.join(HERE, "_ref", f"libref{prec}.so")
+    def __init__(self, prec: int, shim: bool = False):
+        path = _ref_path(prec, shim)
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         self.prec = prec

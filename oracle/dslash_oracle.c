@@ -338,56 +338,101 @@ void orc_tables_free(orc_tables *t)
     free(t->site_table); free(t->bwd); free(t->fwd); free(t);
 }
 
-/* One template, instantiated for float and double arithmetic. */
-#define ORC_PORT(REAL, NAME)                                                        \
-typedef struct { REAL re, im; } NAME##_c;                                            \
-static inline NAME##_c NAME##_mul(NAME##_c a, NAME##_c b)                            \
-{ NAME##_c r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; return r; }   \
-static inline NAME##_c NAME##_cjmul(NAME##_c a, NAME##_c b) /* conj(a) * b */        \
-{ NAME##_c r = {a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re}; return r; }   \
-/* coef codes: 0:+1 1:-1 2:+i 3:-i */                                                \
-static inline NAME##_c NAME##_scale(NAME##_c a, int code)                            \
+/* Spin projection (1 - sigma*gamma_mu) psi for sigma = +1, in half-spinor form:
+ *   h0 = psi0 + a0*psi_j0, h1 = psi1 + a1*psi_j1;   after the SU(3) multiply
+ *   w0, w1 = M h0, M h1 and the lower components are r2 = b2*w_k2, r3 = b3*w_k3.
+ * sigma = -1 flips every coefficient.  Derived from the gamma matrices above. */
+static const struct { int j0, a0, j1, a1, k2, b2, k3, b3; } PROJ[4] = {
+    /* mu=0: h0=psi0-i psi3, h1=psi1-i psi2; r2= i w1, r3= i w0 */ {3, 3, 2, 3, 1, 2, 0, 2},
+    /* mu=1: h0=psi0+psi3,   h1=psi1-psi2;   r2=-w1,   r3= w0   */ {3, 0, 2, 1, 1, 1, 0, 0},
+    /* mu=2: h0=psi0-i psi2, h1=psi1+i psi3; r2= i w0, r3=-i w1 */ {2, 3, 3, 2, 0, 2, 1, 3},
+    /* mu=3: h0=psi0-psi2,   h1=psi1-psi3;   r2=-w0,   r3=-w1   */ {2, 1, 3, 1, 0, 1, 1, 1},
+};
+
+/* One template, instantiated for float and double arithmetic.
+ *
+ * The hop works on 4-wide vectors (GCC vector extensions, portable) that hold
+ * one colour of two spin components as (re, im, re, im): the two upper spin
+ * components of the half spinor, or of the accumulator, or its two lower
+ * ones.  For each direction both projection coefficients are real or both
+ * imaginary, and so are both reconstruction coefficients, so each step is a
+ * lane permutation, a constant sign vector and an add.  The colour multiply
+ * is w_i = sum_j Re(M_ij) h_j + Im(M_ij) (i h_j).                            */
+#define ORC_PORT(REAL, NAME, IREAL)                                                 \
+typedef REAL NAME##_v __attribute__((vector_size(4 * sizeof(REAL))));              \
+typedef IREAL NAME##_m __attribute__((vector_size(4 * sizeof(REAL))));             \
+/* {a.re, a.im, b.re, b.im} of the complex numbers at a and b */                     \
+static inline __attribute__((always_inline))                                       \
+NAME##_v NAME##_pair(const REAL *a, const REAL *b)                                   \
+{ return (NAME##_v){a[0], a[1], b[0], b[1]}; }                                       \
+/* code * v for each complex of v (both codes real or both imaginary):        \
+ * 0: +1, 1: -1, 2: +i, 3: -i                                                  */   \
+static inline __attribute__((always_inline))                                       \
+NAME##_v NAME##_coef(NAME##_v v, const int ca, const int cb)                         \
 {                                                                                    \
-    NAME##_c r;                                                                      \
-    switch (code) {                                                                  \
-    case 0: r = a; break;                                                            \
-    case 1: r.re = -a.re; r.im = -a.im; break;                                       \
-    case 2: r.re = -a.im; r.im = a.re; break;                                        \
-    default: r.re = a.im; r.im = -a.re; break;                                       \
-    }                                                                                \
-    return r;                                                                        \
+    const REAL sar = (ca == 0 || ca == 3) ? 1 : -1, sai = (ca == 0 || ca == 2) ? 1 : -1; \
+    const REAL sbr = (cb == 0 || cb == 3) ? 1 : -1, sbi = (cb == 0 || cb == 2) ? 1 : -1; \
+    if (ca >= 2) v = __builtin_shuffle(v, (NAME##_m){1, 0, 3, 2});                   \
+    return v * (NAME##_v){sar, sai, sbr, sbi};                                       \
 }                                                                                    \
-static void NAME##_hop(NAME##_c acc[4][3], const REAL *psi_site, const REAL *link,   \
-                       int dagger, int mu, int sigma)                                \
+/* always inlined with constant dagger, mu and sigma: the coefficient codes   \
+ * and the PROJ entries fold to constants, as in the reference's one site     \
+ * kernel per direction and sign (lib/site_dslash_32bit_scalar.c:23-3098) */   \
+static inline __attribute__((always_inline))                                       \
+void NAME##_hop(NAME##_v up[3], NAME##_v lo[3], const REAL *ps, const REAL *lk,     \
+                const int dagger, const int mu, const int sigma)                   \
 {                                                                                    \
-    const NAME##_c *ps = (const NAME##_c *)psi_site;                                 \
-    const NAME##_c *lk = (const NAME##_c *)link; /* lk[3*j+i] = U_ij */              \
-    int a0 = PROJ[mu].a0, a1 = PROJ[mu].a1, b2 = PROJ[mu].b2, b3 = PROJ[mu].b3;      \
-    if (sigma < 0) { a0 ^= 1; a1 ^= 1; b2 ^= 1; b3 ^= 1; }                           \
-    NAME##_c h[2][3], w[2][3];                                                       \
+    const int f = sigma < 0;                                                         \
+    const int a0 = PROJ[mu].a0 ^ f, a1 = PROJ[mu].a1 ^ f;                            \
+    const int b2 = PROJ[mu].b2 ^ f, b3 = PROJ[mu].b3 ^ f;                            \
+    const int j0 = PROJ[mu].j0, j1 = PROJ[mu].j1;                                    \
+    NAME##_v h[3], ih[3];                                                            \
     for (int c = 0; c < 3; c++) {                                                    \
-        NAME##_c t0 = NAME##_scale(ps[PROJ[mu].j0 * 3 + c], a0);                     \
-        NAME##_c t1 = NAME##_scale(ps[PROJ[mu].j1 * 3 + c], a1);                     \
-        h[0][c].re = ps[c].re + t0.re;     h[0][c].im = ps[c].im + t0.im;            \
-        h[1][c].re = ps[3 + c].re + t1.re; h[1][c].im = ps[3 + c].im + t1.im;        \
+        /* (h0_c, h1_c) = (psi0_c + a0 psi_j0,c, psi1_c + a1 psi_j1,c) */            \
+        h[c] = NAME##_pair(ps + 2 * c, ps + 6 + 2 * c) +                             \
+               NAME##_coef(NAME##_pair(ps + 6 * j0 + 2 * c, ps + 6 * j1 + 2 * c), a0, a1); \
+        ih[c] = NAME##_coef(h[c], 2, 2);                                             \
     }                                                                                \
-    for (int k = 0; k < 2; k++)                                                      \
-        for (int i = 0; i < 3; i++) {                                                \
-            NAME##_c s = {0, 0};                                                     \
-            for (int j = 0; j < 3; j++) {                                            \
-                NAME##_c p = dagger ? NAME##_cjmul(lk[3 * i + j], h[k][j])           \
-                                    : NAME##_mul(lk[3 * j + i], h[k][j]);            \
-                s.re += p.re; s.im += p.im;                                          \
-            }                                                                        \
-            w[k][i] = s;                                                             \
+    for (int i = 0; i < 3; i++) {                                                    \
+        NAME##_v w = {0, 0, 0, 0};                                                   \
+        for (int j = 0; j < 3; j++) {                                                \
+            /* M = U: M_ij = U_ij = lk[3j+i];  M = U^+: M_ij = conj(U_ji) = conj(lk[3i+j]) */ \
+            const REAL *m = dagger ? lk + 2 * (3 * i + j) : lk + 2 * (3 * j + i);    \
+            w += m[0] * h[j] + (dagger ? -m[1] : m[1]) * ih[j];                      \
         }                                                                            \
+        up[i] += w;                                                                  \
+        /* lower pair (r2, r3) = (b2 w_k2, b3 w_k3); (k2, k3) is (1, 0) or (0, 1) */  \
+        const NAME##_v wl = PROJ[mu].k2 == 1 ? __builtin_shuffle(w, (NAME##_m){2, 3, 0, 1}) : w; \
+        lo[i] += NAME##_coef(wl, b2, b3);                                            \
+    }                                                                                \
+}                                                                                    \
+/* Both hops of direction MU (forward: U_mu(x), backward: U_mu(x-mu)^+) */          \
+static inline __attribute__((always_inline))                                       \
+void NAME##_dir(NAME##_v up[3], NAME##_v lo[3], const orc_tables *t, const REAL *u,  \
+                const REAL *psi, int ix, int site, const int mu, const int sg)      \
+{                                                                                    \
+    int fs = t->fwd[ix * 4 + mu], bs = t->bwd[ix * 4 + mu];                          \
+    NAME##_hop(up, lo, psi + (size_t)fs * 24, u + ((size_t)site * 4 + mu) * 18, 0, mu, sg); \
+    NAME##_hop(up, lo, psi + (size_t)bs * 24, u + ((size_t)bs * 4 + mu) * 18, 1, mu, -sg);  \
+}                                                                                    \
+/* One target site (traversal index ix), the directions unrolled */                 \
+static inline __attribute__((always_inline))                                       \
+void NAME##_site(const orc_tables *t, const REAL *u, const REAL *psi, REAL *res,    \
+                 int ix, int nd, const int sg)                                       \
+{                                                                                    \
+    NAME##_v up[3] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};                    \
+    NAME##_v lo[3] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};                    \
+    int site = t->site_table[ix];                                                    \
+    NAME##_dir(up, lo, t, u, psi, ix, site, 0, sg);                                  \
+    NAME##_dir(up, lo, t, u, psi, ix, site, 1, sg);                                  \
+    NAME##_dir(up, lo, t, u, psi, ix, site, 2, sg);                                  \
+    if (nd == 4) NAME##_dir(up, lo, t, u, psi, ix, site, 3, sg);                     \
+    REAL *r = res + (size_t)site * 24; /* [spin][colour][re, im] */                  \
     for (int c = 0; c < 3; c++) {                                                    \
-        NAME##_c r2 = NAME##_scale(w[PROJ[mu].k2][c], b2);                           \
-        NAME##_c r3 = NAME##_scale(w[PROJ[mu].k3][c], b3);                           \
-        acc[0][c].re += w[0][c].re; acc[0][c].im += w[0][c].im;                      \
-        acc[1][c].re += w[1][c].re; acc[1][c].im += w[1][c].im;                      \
-        acc[2][c].re += r2.re;      acc[2][c].im += r2.im;                           \
-        acc[3][c].re += r3.re;      acc[3][c].im += r3.im;                           \
+        r[2 * c] = up[c][0];      r[2 * c + 1] = up[c][1];                           \
+        r[6 + 2 * c] = up[c][2];  r[6 + 2 * c + 1] = up[c][3];                       \
+        r[12 + 2 * c] = lo[c][0]; r[12 + 2 * c + 1] = lo[c][1];                      \
+        r[18 + 2 * c] = lo[c][2]; r[18 + 2 * c + 1] = lo[c][3];                      \
     }                                                                                \
 }                                                                                    \
 /* Target sites [first, first+count) of checkerboard 1-cb, in traversal order  \
@@ -404,19 +449,12 @@ void orc_dslash_port_range_##NAME(const orc_tables *t, const REAL *u,           
     int lo = target * t->Vh + first, hi = lo + count;                                \
     int nd = t->nd;                                                                  \
     if (nthreads <= 0) nthreads = 1;                                                 \
-    _Pragma("omp parallel for schedule(static) num_threads(nthreads)")               \
-    for (int ix = lo; ix < hi; ix++) {                                               \
-        NAME##_c acc[4][3];                                                          \
-        memset(acc, 0, sizeof(acc));                                                 \
-        int site = t->site_table[ix];                                                \
-        for (int mu = 0; mu < nd; mu++) {                                            \
-            int fs = t->fwd[ix * 4 + mu], bs = t->bwd[ix * 4 + mu];                  \
-            NAME##_hop(acc, psi + (size_t)fs * 24, u + ((size_t)site * 4 + mu) * 18, \
-                       0, mu, isign);                                                \
-            NAME##_hop(acc, psi + (size_t)bs * 24, u + ((size_t)bs * 4 + mu) * 18,   \
-                       1, mu, -isign);                                               \
-        }                                                                            \
-        memcpy(res + (size_t)site * 24, acc, sizeof(acc));                           \
+    if (isign == 1) {                                                                \
+        _Pragma("omp parallel for schedule(static) num_threads(nthreads)")           \
+        for (int ix = lo; ix < hi; ix++) NAME##_site(t, u, psi, res, ix, nd, 1);     \
+    } else {                                                                         \
+        _Pragma("omp parallel for schedule(static) num_threads(nthreads)")           \
+        for (int ix = lo; ix < hi; ix++) NAME##_site(t, u, psi, res, ix, nd, -1);    \
     }                                                                                \
 }                                                                                    \
 void orc_dslash_port_##NAME(const orc_tables *t, const REAL *u, const REAL *psi,     \
@@ -425,19 +463,8 @@ void orc_dslash_port_##NAME(const orc_tables *t, const REAL *u, const REAL *psi,
     orc_dslash_port_range_##NAME(t, u, psi, res, isign, cb, 0, t->Vh, nthreads);     \
 }
 
-/* Spin projection (1 - sigma*gamma_mu) psi for sigma = +1, in half-spinor form:
- *   h0 = psi0 + a0*psi_j0, h1 = psi1 + a1*psi_j1;   after the SU(3) multiply
- *   w0, w1 = M h0, M h1 and the lower components are r2 = b2*w_k2, r3 = b3*w_k3.
- * sigma = -1 flips every coefficient.  Derived from the gamma matrices above. */
-static const struct { int j0, a0, j1, a1, k2, b2, k3, b3; } PROJ[4] = {
-    /* mu=0: h0=psi0-i psi3, h1=psi1-i psi2; r2= i w1, r3= i w0 */ {3, 3, 2, 3, 1, 2, 0, 2},
-    /* mu=1: h0=psi0+psi3,   h1=psi1-psi2;   r2=-w1,   r3= w0   */ {3, 0, 2, 1, 1, 1, 0, 0},
-    /* mu=2: h0=psi0-i psi2, h1=psi1+i psi3; r2= i w0, r3=-i w1 */ {2, 3, 3, 2, 0, 2, 1, 3},
-    /* mu=3: h0=psi0-psi2,   h1=psi1-psi3;   r2=-w0,   r3=-w1   */ {2, 1, 3, 1, 0, 1, 1, 1},
-};
-
-ORC_PORT(float, f32)
-ORC_PORT(double, f64)
+ORC_PORT(float, f32, int)
+ORC_PORT(double, f64, long long)
 
 int orc_max_threads(void)
 {
