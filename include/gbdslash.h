@@ -280,6 +280,40 @@ int gbds_op_force(gbds_op op, const void *gauge, const void *psi, const void *ch
                   double coef, int accumulate, void *force_packed, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Time direction split across ranks (domain decomposition)                  */
+/* ------------------------------------------------------------------------ */
+/* Replaces the reference's parscalar halo exchange
+ * (lib/sse_su3dslash_32bit_parscalar.c:967-1095 face buffers, :1203-1284
+ * communication overlapped with the interior; lib/shift_tables_parscalar.c).
+ * The operator of gbds_op_create is one rank's sub-lattice dims[4], with the
+ * global lattice split into equal slabs along t (dims[3] even, so local and
+ * global parities agree); x, y and z stay periodic within the rank.  Per
+ * application:
+ *   1. gbds_op_pack_faces fills the two send buffers from the source psi
+ *      (checkerboard cb):
+ *        to_prev: (1 - isign g_t) psi on the first local time slice, the
+ *                 previous rank's forward t hops (12 reals a face site);
+ *        to_next: U_t^+ (1 + isign g_t) psi on the last local time slice,
+ *                 the next rank's backward t hops (the sender owns U_t);
+ *   2. the caller moves to_prev to the previous rank's from_next and to_next
+ *      to the next rank's from_prev (NCCL send/recv, MPI, peer copies; a
+ *      single rank passes its own buffers across);
+ *   3. gbds_op_dslash_halo computes res on checkerboard 1-cb; part
+ *      GBDS_HALO_INTERIOR needs no face and can run while the faces travel,
+ *      GBDS_HALO_BOUNDARY then does the first and last time slices,
+ *      GBDS_HALO_ALL does both in one launch.
+ * Face buffers: gbds_op_face_bytes each, 16-byte aligned, device memory.
+ * Needs a 4D, single right-hand side, native-format operator. */
+#define GBDS_HALO_ALL 0
+#define GBDS_HALO_INTERIOR 1
+#define GBDS_HALO_BOUNDARY 2
+size_t gbds_op_face_bytes(gbds_op op);
+int gbds_op_pack_faces(gbds_op op, const void *gauge, const void *psi, int isign, int cb, void *to_prev,
+                       void *to_next, void *stream);
+int gbds_op_dslash_halo(gbds_op op, const void *gauge, const void *psi, const void *from_prev, const void *from_next,
+                        void *res, int isign, int cb, int part, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Even-odd preconditioned Wilson solver                                     */
 /* ------------------------------------------------------------------------ */
 /* M = 1 - kappa^2 D_eo D_oe on checkerboard 0 (even sites), D the operator

@@ -101,6 +101,10 @@ def core() -> ctypes.CDLL:
     L.gbds_bsolver_set_gauge.argtypes = [vp, vp, vp]
     L.gbds_bsolver_solve.argtypes = [vp, vp, vp, ctypes.POINTER(SolverStats), vp]
     L.gbds_op_force.argtypes = [vp, vp, vp, vp, i, i, i, ctypes.c_double, i, vp, vp]
+    L.gbds_op_face_bytes.argtypes = [vp]
+    L.gbds_op_face_bytes.restype = sz
+    L.gbds_op_pack_faces.argtypes = [vp, vp, vp, i, i, vp, vp, vp]
+    L.gbds_op_dslash_halo.argtypes = [vp, vp, vp, vp, vp, vp, i, i, i, vp]
     L.gbds_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(BatchItem), i, i, i]
     L.gbds_batch_destroy.argtypes = [vp]
     L.gbds_batch_set_schedule.argtypes = [vp, i, i, i]

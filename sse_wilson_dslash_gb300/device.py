@@ -161,6 +161,41 @@ class DslashOperator:
                                              1 if accumulate else 0, ctypes.c_void_p(_dptr(out)), _stream(stream)))
         return out
 
+    # -- time direction split across ranks (gbds_op_pack_faces / _dslash_halo) ---
+    HALO_PARTS = {"all": 0, "interior": 1, "boundary": 2}
+
+    @property
+    def face_bytes(self) -> int:
+        """Bytes of one face buffer (one checkerboard of a time slice, 12 reals a site)."""
+        return int(_lib.core().gbds_op_face_bytes(self._h))
+
+    def new_face(self):
+        import torch
+        return torch.empty(self.face_bytes, dtype=torch.uint8, device=self.device)
+
+    def pack_faces(self, gauge, psi, isign: int, cb: int, to_prev, to_next, stream=None):
+        """Send buffers of the source psi (checkerboard cb) when t is split
+        across ranks: to_prev = (1 - isign g_t) psi on the first time slice,
+        to_next = U_t^+ (1 + isign g_t) psi on the last one."""
+        for t in (to_prev, to_next):
+            if t.numel() * t.element_size() < self.face_bytes:
+                raise ValueError("face buffer too small")
+        _lib.check(_lib.core().gbds_op_pack_faces(self._h, ctypes.c_void_p(_dptr(gauge)), ctypes.c_void_p(_dptr(psi)),
+                                                  int(isign), int(cb), ctypes.c_void_p(_dptr(to_prev)),
+                                                  ctypes.c_void_p(_dptr(to_next)), _stream(stream)))
+
+    def apply_halo(self, gauge, psi, from_prev, from_next, isign: int, cb: int, out=None, part: str = "all",
+                   stream=None):
+        """out (checkerboard 1-cb) = Dslash psi with the t hops across the slab
+        boundaries taken from the received faces; part 'interior' needs none."""
+        out = self.new_spinor() if out is None else out
+        fp = ctypes.c_void_p(_dptr(from_prev)) if from_prev is not None else None
+        fn = ctypes.c_void_p(_dptr(from_next)) if from_next is not None else None
+        _lib.check(_lib.core().gbds_op_dslash_halo(self._h, ctypes.c_void_p(_dptr(gauge)), ctypes.c_void_p(_dptr(psi)),
+                                                   fp, fn, ctypes.c_void_p(_dptr(out)), int(isign), int(cb),
+                                                   self.HALO_PARTS[part], _stream(stream)))
+        return out
+
     def _check_real(self, t, n):
         if t.dtype != self.real_dtype:
             raise TypeError(f"expected {self.real_dtype}")
