@@ -18,7 +18,8 @@ line on rank 0:
   cpu_baseline the oracle's table-driven port (OpenMP) on the host cores, on a
               bounded slice of the same workload
   variants    recon-12, FP64, the 3D operator on 24^3x48, several right-hand
-              sides on 24^3x48, the uneven batch, the force (not the headline)
+              sides on 24^3x48, the uneven batch, the force, one rank's slab
+              of the lattice split along t (not the headline)
 
 --impl reference times the CPU implementation of the path on the host cores:
 the reference library built from its own sources (oracle/_ref) where it was
@@ -464,6 +465,60 @@ def force_variants(torch, peak, steps):
     return out
 
 
+def split_t_variant(torch, peak, steps):
+    """One rank's slab when 32^3x64 is split along t across two GPUs: the
+    32^3x32 slab's periodic Dslash against the split form (pack the two send
+    faces, move them -- here a device copy stands in for the transfer between
+    GPUs --, the interior time slices, then the two boundary slices), FP32,
+    18-real links, CUDA events over `steps` applications of each."""
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims = (32, 32, 32, 32)
+    op = DslashOperator(dims, nd=4, prec=32, recon=18)
+    u, psi = make_fields(dims, torch.float32, torch, seed=31)
+    gauge = op.pack_gauge(u)
+    src = op.pack_spinor(psi, 0)
+    del u, psi
+    out = op.new_spinor()
+    faces = [op.new_face() for _ in range(4)]
+    stream = torch.cuda.current_stream()
+
+    def periodic():
+        op.apply(gauge, src, 1, 0, out=out, stream=stream)
+
+    def split():
+        op.pack_faces(gauge, src, 1, 0, faces[0], faces[1], stream=stream)
+        faces[3].copy_(faces[0])
+        faces[2].copy_(faces[1])
+        op.apply_halo(gauge, src, None, None, 1, 0, out=out, part="interior", stream=stream)
+        op.apply_halo(gauge, src, faces[2], faces[3], 1, 0, out=out, part="boundary", stream=stream)
+
+    def timed(fn, n):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    n = max(20, min(steps, 200))
+    ms_p = timed(periodic, n)
+    ms_s = timed(split, n)
+    ms_pack = timed(lambda: op.pack_faces(gauge, src, 1, 0, faces[0], faces[1], stream=stream), n)
+    sites = op.volume_cb
+    res = {"slab": list(dims), "of_lattice": [32, 32, 32, 64], "ranks": 2,
+           "periodic_ms": ms_p, "split_ms": ms_s, "pack_faces_ms": ms_pack,
+           "split_gflops": 1320 * sites / (ms_s * 1e6),
+           "split_roofline_frac": op.bytes_per_site * sites / (ms_s * 1e6) / peak,
+           "face_bytes": op.face_bytes, "faces_per_rank_per_application": 2}
+    del gauge, src, out, faces
+    op.close()
+    torch.cuda.empty_cache()
+    return res
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -744,6 +799,8 @@ def run_gb300(args):
             variants["uneven_batch"] = uneven_batch(torch, peak)
         if run("force"):
             variants.update(force_variants(torch, peak, vsteps))
+        if run("split_t"):
+            variants["split_t_32x32x32x64_2ranks_f32"] = split_t_variant(torch, peak, vsteps)
 
     solver = None
     if not args.no_solver:
@@ -838,7 +895,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true")
     ap.add_argument("--variants", default="all",
-                    help="comma list of variant sections: recon12, f64, 3d, multi_rhs, uneven_batch, force (default all)")
+                    help="comma list of variant sections: recon12, f64, 3d, multi_rhs, uneven_batch, force, split_t (default all)")
     ap.add_argument("--tuning", default=None,
                     help="block,variant of the headline kernel instead of autotuning (for profiling runs)")
     ap.add_argument("--dims", default=None,

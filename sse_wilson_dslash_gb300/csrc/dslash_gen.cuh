@@ -666,6 +666,157 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// The fully packed hop with two right-hand sides per thread (variant 3):
+// rhs r and r + NRHS / 2 of one site share every staged link splat, so each
+// shared-memory load of M serves two outputs (half the broadcast wavefronts
+// of variant 2), and each thread has two independent chains in flight.
+// ---------------------------------------------------------------------------
+
+template <int MU, int SIG, bool SCALE>
+__device__ __forceinline__ void packed_project(const float (&v)[24], float nrm, float2 (&R)[3], float2 (&I)[3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIG > 0 ? 0 : 1;
+    using A0 = CPart<P::a0 ^ f>;
+    using A1 = CPart<P::a1 ^ f>;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int s0 = 2 * c, s1 = 2 * (3 + c), j0 = 2 * (3 * P::j0 + c), j1 = 2 * (3 * P::j1 + c);
+        R[c] = __ffma2_rn(make_float2(v[j0 + (A0::swap ? 1 : 0)], v[j1 + (A1::swap ? 1 : 0)]),
+                          make_float2(A0::sre, A1::sre), make_float2(v[s0], v[s1]));
+        I[c] = __ffma2_rn(make_float2(v[j0 + (A0::swap ? 0 : 1)], v[j1 + (A1::swap ? 0 : 1)]),
+                          make_float2(A0::sim, A1::sim), make_float2(v[s0 + 1], v[s1 + 1]));
+        if constexpr (SCALE) {
+            R[c] = __fmul2_rn(R[c], make_float2(nrm, nrm));
+            I[c] = __fmul2_rn(I[c], make_float2(nrm, nrm));
+        }
+    }
+}
+
+// Both rhs of a thread: multiply by the staged M (each splat loaded once) and
+// add into the upper and lower pairs, as packed_hop does for one rhs.
+template <int MU, int SIG, int LORD>
+__device__ __forceinline__ void packed_mul_recon2(const float4 *M, const float2 (&R)[2][3], const float2 (&I)[2][3],
+                                                  float2 (&UR)[2][3], float2 (&UI)[2][3], float2 (&LR)[2][3],
+                                                  float2 (&LI)[2][3]) {
+    using P = Proj<MU>;
+    constexpr int f = SIG > 0 ? 0 : 1;
+    using B2 = CPart<P::b2 ^ f>;
+    using B3 = CPart<P::b3 ^ f>;
+    static_assert(B2::swap == B3::swap, "both halves take the same parts");
+    static_assert(LORD == 0 ? (P::k2 == 0 && P::k3 == 1) : (P::k2 == 1 && P::k3 == 0), "lower pair order");
+    using X = std::conditional_t<LORD == 0, B2, B3>;
+    using Y = std::conditional_t<LORD == 0, B3, B2>;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float2 ar[2], br[2], ai[2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) ar[q] = br[q] = ai[q] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const float4 m = M[i * 3 + j];
+            const float2 mr = make_float2(m.x, m.y), mi = make_float2(m.z, m.w);
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                ar[q] = __ffma2_rn(mr, R[q][j], ar[q]);
+                br[q] = __ffma2_rn(mi, I[q][j], br[q]);
+                ai[q] = __ffma2_rn(mr, I[q][j], ai[q]);
+                ai[q] = __ffma2_rn(mi, R[q][j], ai[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const float2 wr = __ffma2_rn(br[q], make_float2(-1.f, -1.f), ar[q]);
+            UR[q][i] = __fadd2_rn(UR[q][i], wr);
+            UI[q][i] = __fadd2_rn(UI[q][i], ai[q]);
+            LR[q][i] = __ffma2_rn(B2::swap ? ai[q] : wr, make_float2(X::sre, Y::sre), LR[q][i]);
+            LI[q][i] = __ffma2_rn(B2::swap ? wr : ai[q], make_float2(X::sim, Y::sim), LI[q][i]);
+        }
+    }
+}
+
+template <int FMT, int RECON, int ISIGN, int NRHS>
+__global__ void __launch_bounds__(128, 3) dslash_gen4_kernel(const GenArgs a) {
+    static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
+    pdl_allow_next();
+    pdl_wait_prev();
+    constexpr int H = NRHS / 2;    // threads per site
+    constexpr int P = 128 / H;     // sites per CTA
+    constexpr bool SCALE = FMT == kFmtF16N;
+    __shared__ float4 sL[P][8][9];
+    const int t = threadIdx.x;
+    const int p = t / H, r = t % H;  // this thread: rhs r and r + H of site p
+    const int h = blockIdx.x * P + p;
+    const bool act = h < a.g.Vh;
+    Nbr n;
+    if (act) neighbours<4>(a.g, h, a.pt, n);
+    // links l = r, r + H, ... < 8 of the site (H = 4 threads a site for 8 rhs):
+    // direction l / 2, forward (even l) or backward
+    for (int l = r; act && l < 8; l += H) {
+        const int mu = l >> 1;
+        const bool bwd = l & 1;
+        const int nbm = mu == 0 ? n.b[0] : (mu == 1 ? n.b[1] : (mu == 2 ? n.b[2] : n.b[3]));
+        const int lp = bwd ? 1 - a.pt : a.pt;
+        cx<float> U[3][3];
+        Field<float>::template load_link<RECON>(a.gauge + (size_t)(lp * 4 + mu) * a.link_block_bytes, a.g.stride,
+                                                bwd ? nbm : h, U);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                // forward: M_ij = U_ij; backward: M_ij = conj(U_ji)
+                const float mr = bwd ? U[j][i].r : U[i][j].r;
+                const float mi = bwd ? -U[j][i].i : U[i][j].i;
+                sL[p][l][i * 3 + j] = make_float4(mr, mr, mi, mi);
+            }
+    }
+    __syncthreads();
+    if (!act) return;
+    float2 UR[2][3], UI[2][3], LR[2][3], LI[2][3];
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) UR[q][c] = UI[q][c] = LR[q][c] = LI[q][c] = make_float2(0.f, 0.f);
+#define GBDS_G4_HOP(MU, LORD, NB, SIG, L)                                                              \
+    {                                                                                                  \
+        float2 R[2][3], I[2][3];                                                                       \
+        _Pragma("unroll") for (int q = 0; q < 2; q++) {                                               \
+            float v[24];                                                                               \
+            const float sc = load_reals<FMT>(a.psi, a.cs, (size_t)(NB) * NRHS + r + q * H, v);         \
+            packed_project<MU, SIG, SCALE>(v, sc, R[q], I[q]);                                         \
+        }                                                                                              \
+        packed_mul_recon2<MU, SIG, LORD>(sL[p][L], R, I, UR, UI, LR, LI);                              \
+    }
+#define GBDS_G4_DIR(MU, LORD)                                   \
+    GBDS_G4_HOP(MU, LORD, n.f[MU], ISIGN, 2 * MU)               \
+    GBDS_G4_HOP(MU, LORD, n.b[MU], -ISIGN, 2 * MU + 1)
+    GBDS_G4_DIR(0, 1)
+    GBDS_G4_DIR(1, 1)
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            LR[q][c] = make_float2(LR[q][c].y, LR[q][c].x);
+            LI[q][c] = make_float2(LI[q][c].y, LI[q][c].x);
+        }
+    GBDS_G4_DIR(2, 0)
+    GBDS_G4_DIR(3, 0)
+#undef GBDS_G4_DIR
+#undef GBDS_G4_HOP
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        cx<float> acc[4][3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            acc[0][c] = {UR[q][c].x, UI[q][c].x};
+            acc[1][c] = {UR[q][c].y, UI[q][c].y};
+            acc[2][c] = {LR[q][c].x, LI[q][c].x};
+            acc[3][c] = {LR[q][c].y, LI[q][c].y};
+        }
+        Sio<FMT>::store(a.res, a.cs, (size_t)h * NRHS + r + q * H, acc);
+    }
+}
+
 // One thread per (site, rhs); 4D.  EPI = 1 adds the xpay epilogue
 // (res = x + coef * D psi) with one |res|^2 partial per block; EPI = 2 the
 // same with one partial per block and rhs (NRHS 2..32, 128-thread blocks).

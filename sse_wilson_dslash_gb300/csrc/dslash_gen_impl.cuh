@@ -106,6 +106,16 @@ void launch_gen3_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
     }
 }
 
+template <int FMT, int RECON, int ISIGN>
+void launch_gen4_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
+    const unsigned vh = (unsigned)a.g.Vh;
+    switch (nrhs) {
+    case 8: launch_pdl(dslash_gen4_kernel<FMT, RECON, ISIGN, 8>, dim3((vh + 31) / 32), 128, st, a); break;
+    case 16: launch_pdl(dslash_gen4_kernel<FMT, RECON, ISIGN, 16>, dim3((vh + 15) / 16), 128, st, a); break;
+    default: launch_pdl(dslash_gen4_kernel<FMT, RECON, ISIGN, 32>, dim3((vh + 7) / 8), 128, st, a); break;
+    }
+}
+
 template <int FMT>
 cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
                          int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0) {
@@ -131,10 +141,17 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     // variant 2 (fully packed: 16-bit and FP32-pair storage; its xpay
     // epilogue serves the batched solver's FP32-pair fields); like variant 1,
     // it falls back to the plain kernel otherwise
-    const bool v3 = variant == 2 && packed_nrhs && FMT != kFmtNative && (FMT == kFmtF32Pairs || !epi);
+    const bool v3 = (variant == 2 || variant == 3) && packed_nrhs && FMT != kFmtNative && (FMT == kFmtF32Pairs || !epi);
+    // variant 3: the fully packed kernel with two rhs per thread (no
+    // epilogue; with one, variant 2 runs)
+    const bool v4 = variant == 3 && packed_nrhs && FMT != kFmtNative && !epi;
 #define GBDS_GEN(R, S)                                                   \
     do {                                                                 \
         if constexpr (FMT != kFmtNative) {                               \
+            if (v4) {                                                    \
+                launch_gen4_nrhs<FMT, R, S>(a, nrhs, st);                \
+                break;                                                   \
+            }                                                            \
             if (v3) {                                                    \
                 if constexpr (FMT == kFmtF32Pairs) {                     \
                     if (epi) launch_gen3_nrhs<FMT, R, S, 2>(a, nrhs, st); \
