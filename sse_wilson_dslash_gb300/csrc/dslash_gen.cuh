@@ -736,7 +736,7 @@ __device__ __forceinline__ void packed_mul_recon2(const float4 *M, const float2 
 }
 
 template <int FMT, int RECON, int ISIGN, int NRHS>
-__global__ void __launch_bounds__(128, 3) dslash_gen4_kernel(const GenArgs a) {
+__global__ void __launch_bounds__(128, 4) dslash_gen4_kernel(const GenArgs a) {
     static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
     pdl_allow_next();
     pdl_wait_prev();
