@@ -165,9 +165,12 @@ int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
  * multi-RHS kernel, 1 = the packed FP32x2 form (8, 16, 32 rhs; the block
  * size is fixed at 128), and for the 16-bit and FP32-pair formats 2 =
  * projection, multiply and reconstruction all in packed FP32x2 (8, 16, 32
- * rhs; 128-thread blocks), and 3 = variant 2 with two rhs per thread, which
- * share each staged link (the default from 16 rhs on).  Variants 1 to 3 run
- * the plain kernel for other counts of rhs.
+ * rhs; 128-thread blocks), 3 = variant 2 with two rhs per thread, which
+ * share each staged link (the default from 16 rhs on for half + norm and
+ * FP32 pairs), and for the 16-bit formats 4 = variant 3 with each thread's
+ * neighbour spinors prefetched two hops ahead by cp.async into shared memory
+ * (the default from 16 rhs on for bfloat16).  Variants 1 to 4 run the plain
+ * kernel for other counts of rhs (variant 4 on FP32 pairs runs variant 3).
  * gbds_op_num_variants gives the count.  Used by the autotuner. */
 int gbds_op_set_tuning(gbds_op op, int threads, int variant);
 int gbds_op_get_tuning(gbds_op op, int *threads, int *variant);
@@ -181,8 +184,8 @@ int gbds_op_num_variants(gbds_op op);
  * plain multi-RHS kernel, 1 the colour multiply in packed FP32x2 arithmetic
  * on links staged per CTA (8, 16 or 32 rhs), for the 16-bit and FP32-pair
  * formats 2 the whole hop in packed FP32x2 (8, 16, 32 rhs), 3 the same with
- * two rhs per thread and, for 16-bit formats with 16 or 32 rhs, the
- * tensor-core kernel
+ * two rhs per thread, for the 16-bit formats 4 (3 with cp.async prefetching)
+ * and, for 16-bit formats with 16 or 32 rhs, the tensor-core kernel
  * (gbds_op_set_tensor_cores).  Synchronises `stream`. */
 int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream);
 

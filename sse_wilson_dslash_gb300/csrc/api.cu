@@ -126,9 +126,11 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     // storage); from 16 rhs on (at 24^3x48) 2 is fastest where it exists and
     // 1 for FP32 (autotune chooses per shape).
     const bool gen = nrhs > 1 || format != GBDS_SPINOR_NATIVE;
-    // from 16 rhs on: the fully packed kernel with two rhs a thread (variant
-    // 3) for 16-bit and FP32-pair storage, the packed multiply (1) for FP32
-    const int gen_variant = nrhs >= 16 ? (format != GBDS_SPINOR_NATIVE ? 3 : 1) : 0;
+    // from 16 rhs on: for bfloat16 the fully packed kernel with two rhs a
+    // thread and cp.async prefetching (variant 4), for half + norm and FP32
+    // pairs the same without prefetching (3), for FP32 the packed multiply (1)
+    const int gen_variant =
+        nrhs >= 16 ? (format == GBDS_SPINOR_BF16 ? 4 : (format != GBDS_SPINOR_NATIVE ? 3 : 1)) : 0;
     o->variant = gen ? gen_variant : ((prec == 32 && recon == 18) ? 1 : 0);
     o->tensor_cores = 0;
     o->d_err = nullptr;
@@ -252,7 +254,9 @@ extern "C" int gbds_op_set_tuning(gbds_op op, int threads, int variant) {
 
 extern "C" int gbds_op_num_variants(gbds_op op) {
     if (!op) return 0;
-    if (op->format != GBDS_SPINOR_NATIVE) return 4;  // 2: the fully packed kernel; 3: the same, two rhs a thread
+    // 2: the fully packed kernel; 3: the same, two rhs a thread; 4: 3 with
+    // cp.async prefetching (16-bit storage)
+    if (op->format != GBDS_SPINOR_NATIVE) return 5;
     return op->nrhs > 1 ? 2 : dslash_variants(op->prec);
 }
 
@@ -270,8 +274,9 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
     if (!op) return set_error(GBDS_ERROR_NOT_INITIALIZED, "op is NULL");
     // several right-hand sides: the candidates are the plain kernel, its
     // packed FP32x2 form (8, 16, 32 rhs), for 16-bit and FP32-pair storage the
-    // fully packed kernel with one and with two rhs a thread and, for 16-bit
-    // storage with 16 or 32 rhs, the tensor-core kernel
+    // fully packed kernel with one and with two rhs a thread, for 16-bit
+    // storage the latter with cp.async prefetching and, with 16 or 32 rhs,
+    // the tensor-core kernel
     const bool v2ok = op->nrhs == 8 || op->nrhs == 16 || op->nrhs == 32;
     if (generic(op) && !tc_eligible(op) && !v2ok) return GBDS_SUCCESS;
     const std::array<int, 9> key = {op->g.L[0], op->g.L[1], op->g.L[2], op->g.L[3], op->g.nd,
@@ -293,6 +298,7 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
         if (v2ok && op->format != GBDS_SPINOR_NATIVE) {
             cand.push_back({op->block, 2, 0});
             cand.push_back({op->block, 3, 0});
+            if (op->format != GBDS_SPINOR_F32_PAIRS) cand.push_back({op->block, 4, 0});
         }
         if (tc_eligible(op)) cand.push_back({op->block, 0, 1});
     } else {

@@ -817,6 +817,175 @@ __global__ void __launch_bounds__(128, 4) dslash_gen4_kernel(const GenArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Variant 4 (16-bit storage): variant 3 with the neighbour spinors prefetched
+// two hops ahead by cp.async into a per-thread ring of three shared-memory
+// slots, so that up to three hops' loads are in flight without holding
+// registers (variant 3 is latency-bound at four CTAs per SM).  Slot s, rhs q,
+// 16-byte chunk c of thread t at ring[((s * 2 + q) * 3 + c) * 128 + t]
+// (consecutive threads, consecutive 16 bytes); the half + norm format's
+// norms follow.  Every thread reads back only what it copied itself, after
+// its own cp.async.wait_group, and refills a slot one hop after reading it.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_addr_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp_async_16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <int FMT, int NRHS>
+struct G5Smem {
+    static constexpr int P = 256 / NRHS;  // sites per 128-thread CTA (two rhs a thread)
+    static constexpr size_t link_bytes = (size_t)P * 8 * 9 * 16;
+    static constexpr size_t ring_bytes = (size_t)3 * 2 * 3 * 128 * 16;
+    static constexpr size_t norm_bytes = FMT == kFmtF16N ? (size_t)3 * 2 * 128 * 4 : 0;
+    static constexpr size_t bytes = link_bytes + ring_bytes + norm_bytes;
+};
+
+// Copy hop K's two neighbour spinors of this thread into ring slot S.
+template <int FMT, int NRHS, int K, int S>
+__device__ __forceinline__ void g5_issue(const GenArgs &a, const Nbr &n, int r, uint4 *ring, float *rnorm) {
+    constexpr int H = NRHS / 2;
+    const int nb = (K & 1) ? n.b[K >> 1] : n.f[K >> 1];
+    const uint4 *src = reinterpret_cast<const uint4 *>(a.psi);
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const size_t i = (size_t)nb * NRHS + r + q * H;
+#pragma unroll
+        for (int c = 0; c < 3; c++) cp_async_16(ring + ((S * 2 + q) * 3 + c) * 128 + t, src + c * a.cs + i);
+        if constexpr (FMT == kFmtF16N) cp_async_4(rnorm + (S * 2 + q) * 128 + t, Sio<kFmtF16N>::norms(a.psi, a.cs) + i);
+    }
+}
+
+// The 24 reals of rhs q from ring slot S (as load_reals); returns the scale.
+template <int FMT, int S>
+__device__ __forceinline__ float g5_read(const uint4 *ring, const float *rnorm, int q, float (&v)[24]) {
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const uint4 w4 = ring[((S * 2 + q) * 3 + k) * 128 + t];
+        const unsigned w[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            if constexpr (FMT == kFmtBF16) {
+                v[8 * k + 2 * c] = __uint_as_float(w[c] << 16);
+                v[8 * k + 2 * c + 1] = __uint_as_float(w[c] & 0xffff0000u);
+            } else {
+                const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[c]));
+                v[8 * k + 2 * c] = f.x;
+                v[8 * k + 2 * c + 1] = f.y;
+            }
+        }
+    }
+    if constexpr (FMT == kFmtF16N) return rnorm[(S * 2 + q) * 128 + t];
+    else return 1.f;
+}
+
+template <int FMT, int RECON, int ISIGN, int NRHS>
+__global__ void __launch_bounds__(128, 4) dslash_gen5_kernel(const GenArgs a) {
+    static_assert(FMT == kFmtBF16 || FMT == kFmtF16N, "16-bit storage");
+    static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
+    pdl_allow_next();
+    pdl_wait_prev();
+    using SM = G5Smem<FMT, NRHS>;
+    constexpr int H = NRHS / 2;
+    constexpr int P = SM::P;
+    constexpr bool SCALE = FMT == kFmtF16N;
+    extern __shared__ __align__(16) unsigned char g5s[];
+    float4 (*sL)[8][9] = reinterpret_cast<float4 (*)[8][9]>(g5s);
+    uint4 *ring = reinterpret_cast<uint4 *>(g5s + SM::link_bytes);
+    float *rnorm = reinterpret_cast<float *>(g5s + SM::link_bytes + SM::ring_bytes);
+    const int t = threadIdx.x;
+    const int p = t / H, r = t % H;
+    const int h = blockIdx.x * P + p;
+    const bool act = h < a.g.Vh;
+    Nbr n;
+    if (act) neighbours<4>(a.g, h, a.pt, n);
+    // hops 0 and 1 in flight during the link staging
+    if (act) g5_issue<FMT, NRHS, 0, 0>(a, n, r, ring, rnorm);
+    cp_async_commit();
+    if (act) g5_issue<FMT, NRHS, 1, 1>(a, n, r, ring, rnorm);
+    cp_async_commit();
+    for (int l = r; act && l < 8; l += H) {
+        const int mu = l >> 1;
+        const bool bwd = l & 1;
+        const int nbm = mu == 0 ? n.b[0] : (mu == 1 ? n.b[1] : (mu == 2 ? n.b[2] : n.b[3]));
+        const int lp = bwd ? 1 - a.pt : a.pt;
+        cx<float> U[3][3];
+        Field<float>::template load_link<RECON>(a.gauge + (size_t)(lp * 4 + mu) * a.link_block_bytes, a.g.stride,
+                                                bwd ? nbm : h, U);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const float mr = bwd ? U[j][i].r : U[i][j].r;
+                const float mi = bwd ? -U[j][i].i : U[i][j].i;
+                sL[p][l][i * 3 + j] = make_float4(mr, mr, mi, mi);
+            }
+    }
+    __syncthreads();
+    if (!act) {
+        cp_async_wait<0>();
+        return;
+    }
+    float2 UR[2][3], UI[2][3], LR[2][3], LI[2][3];
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) UR[q][c] = UI[q][c] = LR[q][c] = LI[q][c] = make_float2(0.f, 0.f);
+    // hop K = 2 mu + (0 forward, 1 backward) from slot K % 3; then slot
+    // (K + 2) % 3, read during hop K - 1, takes hop K + 2
+#define GBDS_G5_HOP(K, MU, LORD, SIG)                                                             \
+    {                                                                                             \
+        cp_async_wait<1>();                                                                       \
+        float2 R[2][3], I[2][3];                                                                  \
+        _Pragma("unroll") for (int q = 0; q < 2; q++) {                                          \
+            float v[24];                                                                          \
+            const float sc = g5_read<FMT, (K) % 3>(ring, rnorm, q, v);                            \
+            packed_project<MU, SIG, SCALE>(v, sc, R[q], I[q]);                                    \
+        }                                                                                         \
+        if constexpr ((K) + 2 < 8) g5_issue<FMT, NRHS, ((K) + 2) & 7, ((K) + 2) % 3>(a, n, r, ring, rnorm); \
+        cp_async_commit();                                                                        \
+        packed_mul_recon2<MU, SIG, LORD>(sL[p][K], R, I, UR, UI, LR, LI);                         \
+    }
+    GBDS_G5_HOP(0, 0, 1, ISIGN)
+    GBDS_G5_HOP(1, 0, 1, -ISIGN)
+    GBDS_G5_HOP(2, 1, 1, ISIGN)
+    GBDS_G5_HOP(3, 1, 1, -ISIGN)
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            LR[q][c] = make_float2(LR[q][c].y, LR[q][c].x);
+            LI[q][c] = make_float2(LI[q][c].y, LI[q][c].x);
+        }
+    GBDS_G5_HOP(4, 2, 0, ISIGN)
+    GBDS_G5_HOP(5, 2, 0, -ISIGN)
+    GBDS_G5_HOP(6, 3, 0, ISIGN)
+    GBDS_G5_HOP(7, 3, 0, -ISIGN)
+#undef GBDS_G5_HOP
+    cp_async_wait<0>();
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        cx<float> acc[4][3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            acc[0][c] = {UR[q][c].x, UI[q][c].x};
+            acc[1][c] = {UR[q][c].y, UI[q][c].y};
+            acc[2][c] = {LR[q][c].x, LI[q][c].x};
+            acc[3][c] = {LR[q][c].y, LI[q][c].y};
+        }
+        Sio<FMT>::store(a.res, a.cs, (size_t)h * NRHS + r + q * H, acc);
+    }
+}
+
 // One thread per (site, rhs); 4D.  EPI = 1 adds the xpay epilogue
 // (res = x + coef * D psi) with one |res|^2 partial per block; EPI = 2 the
 // same with one partial per block and rhs (NRHS 2..32, 128-thread blocks).

@@ -116,6 +116,28 @@ void launch_gen4_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
     }
 }
 
+// Variant 4 (16-bit storage): dynamic shared memory above the 48 KB default,
+// allowed once per kernel instance before its first launch.
+template <int FMT, int RECON, int ISIGN, int NRHS>
+void launch_gen5_one(const GenArgs &a, cudaStream_t st) {
+    using SM = G5Smem<FMT, NRHS>;
+    auto k = dslash_gen5_kernel<FMT, RECON, ISIGN, NRHS>;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::bytes);
+    if (attr != cudaSuccess) return;  // the error stays the runtime's last error
+    const unsigned vh = (unsigned)a.g.Vh;
+    launch_pdl_smem(k, dim3((vh + SM::P - 1) / SM::P), 128, SM::bytes, st, a);
+}
+
+template <int FMT, int RECON, int ISIGN>
+void launch_gen5_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
+    switch (nrhs) {
+    case 8: launch_gen5_one<FMT, RECON, ISIGN, 8>(a, st); break;
+    case 16: launch_gen5_one<FMT, RECON, ISIGN, 16>(a, st); break;
+    default: launch_gen5_one<FMT, RECON, ISIGN, 32>(a, st); break;
+    }
+}
+
 template <int FMT>
 cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res, int isign,
                          int cb, const void *x, float coef, double *partials, cudaStream_t st, int variant = 0) {
@@ -141,12 +163,21 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     // variant 2 (fully packed: 16-bit and FP32-pair storage; its xpay
     // epilogue serves the batched solver's FP32-pair fields); like variant 1,
     // it falls back to the plain kernel otherwise
-    const bool v3 = (variant == 2 || variant == 3) && packed_nrhs && FMT != kFmtNative && (FMT == kFmtF32Pairs || !epi);
+    const bool v3 = (variant >= 2 && variant <= 4) && packed_nrhs && FMT != kFmtNative &&
+                    (FMT == kFmtF32Pairs || !epi);
     // variant 3: the fully packed kernel with two rhs per thread (no
-    // epilogue; with one, variant 2 runs)
-    const bool v4 = variant == 3 && packed_nrhs && FMT != kFmtNative && !epi;
+    // epilogue; with one, variant 2 runs); variant 4: the same with cp.async
+    // prefetching (16-bit storage; variant 3 for FP32 spin pairs)
+    const bool v5 = variant == 4 && packed_nrhs && (FMT == kFmtBF16 || FMT == kFmtF16N) && !epi;
+    const bool v4 = (variant == 3 || variant == 4) && packed_nrhs && FMT != kFmtNative && !epi;
 #define GBDS_GEN(R, S)                                                   \
     do {                                                                 \
+        if constexpr (FMT == kFmtBF16 || FMT == kFmtF16N) {              \
+            if (v5) {                                                    \
+                launch_gen5_nrhs<FMT, R, S>(a, nrhs, st);                \
+                break;                                                   \
+            }                                                            \
+        }                                                                \
         if constexpr (FMT != kFmtNative) {                               \
             if (v4) {                                                    \
                 launch_gen4_nrhs<FMT, R, S>(a, nrhs, st);                \

@@ -428,11 +428,11 @@ template <> struct Variants<double> { static constexpr int n = 3; static constex
 
 // Launch with the programmatic-serialisation attribute (see pdl_wait_prev).
 template <typename... P, typename... A>
-void launch_pdl(void (*kernel)(P...), dim3 grid, int block, cudaStream_t stream, const A &...args) {
+void launch_pdl_smem(void (*kernel)(P...), dim3 grid, int block, size_t smem, cudaStream_t stream, const A &...args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -442,6 +442,11 @@ void launch_pdl(void (*kernel)(P...), dim3 grid, int block, cudaStream_t stream,
     // a failed launch also sets the runtime's last error, which every
     // launcher returns through cudaGetLastError()
     (void)cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+template <typename... P, typename... A>
+void launch_pdl(void (*kernel)(P...), dim3 grid, int block, cudaStream_t stream, const A &...args) {
+    launch_pdl_smem(kernel, grid, block, 0, stream, args...);
 }
 
 template <typename T, int MINB>
