@@ -457,7 +457,7 @@ def force_variants(torch, peak, steps):
         gbs = nbytes / (ms * 1e6)
         out["force_%s_f%d" % ("x".join(map(str, dims)), prec)] = {
             "ms": ms, "gbs": gbs, "roofline_frac": gbs / peak, "bytes_per_call": nbytes,
-            "links": 4 * V, "launches_per_call": 2, "mode": "su(3) force TA(G U^+)"}
+            "links": 4 * V, "launches_per_call": 1, "mode": "su(3) force TA(G U^+)"}
         del gauge, srcs, f
         op.close()
         torch.cuda.empty_cache()
