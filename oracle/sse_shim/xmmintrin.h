@@ -14,7 +14,7 @@
  * on GCC vector extensions (no x86 instructions, no inline assembly).  Every
  * lane operation is a single IEEE-754 operation in the same order as the SSE
  * instruction; compiled with -ffp-contract=off (no fused multiply-add), the
- * results equal the SSE build's bit for bit, which tests/test_abi.py checks
+ * results equal the SSE build's bit for bit, which tests/test_sse_shim.py checks
  * on x86 hosts where both builds exist.
  *
  * Types: __m128 (4 x float), __m128d (2 x double), __m64 (8 bytes).
