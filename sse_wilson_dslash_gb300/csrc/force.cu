@@ -101,15 +101,18 @@ struct ForceArgs {
 };
 
 // Sites per CTA: 128 in FP32, 64 in FP64, so that the staged output of a CTA
-// (4 links x 18 reals per site) is 36 KB of shared memory either way.
-template <typename T> struct ForceTile { static constexpr int sites = sizeof(T) == 4 ? 128 : 64; };
+// (2 links x 18 reals per site at a time) is 18 KB of shared memory either
+// way; FP32 caps registers for 7 CTAs per SM.
+template <typename T> struct ForceTile {
+    static constexpr int sites = sizeof(T) == 4 ? 128 : 64;
+    static constexpr int min_blocks = sizeof(T) == 4 ? 7 : 1;
+};
 
 // R = G (mode 0) or TA(G U^+) (mode 1) of link (p, h, MU), times coef, into
-// the CTA's staging area at the site's slot: stage[slot*72 + MU*18 + (3j+i)*2]
-// holds R_ij, the packed transposed order of the output.
+// o[(3j+i)*2 + 0/1] = R_ij: the packed transposed order of the output.
 template <typename T, int ISIGN, int MU>
 __device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, const Nbr &n, const cx<T> (&own)[4][3],
-                                           T *stage) {
+                                           T *o) {
     using F = Field<T>;
     using V = typename VecOf<T>::S;
     cx<T> G[3][3];
@@ -145,7 +148,6 @@ __device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, con
             for (int j = 0; j < 3; j++) R[i][j] = G[i][j];
     }
     const T c = (T)a.coef;
-    T *o = stage + MU * 18;
 #pragma unroll
     for (int j = 0; j < 3; j++)
 #pragma unroll
@@ -158,53 +160,46 @@ __device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, con
 // One thread per site of checkerboard p = blockIdx.y (both checkerboards in
 // one launch; they own disjoint links), all four links of the site.  The
 // site's own spinor (chi on checkerboard pt, psi on cb) is loaded once for
-// the four links.  The results are staged in shared memory and written with
-// 16-byte stores: in the canonical layout a CTA's sites are one contiguous
-// run of the packed output, which its threads write in order; with a caller
-// layout each warp writes its sites' 72-real blocks one site at a time.
-template <typename T, int ISIGN>
-__global__ void __launch_bounds__(ForceTile<T>::sites) force_kernel(const ForceArgs a) {
-    using F = Field<T>;
-    using V = typename VecOf<T>::S;
+// the four links.  The results go out in two halves (links 0-1, then 2-3),
+// each staged in shared memory and written with 16-byte stores: in the
+// canonical layout a CTA's sites are one contiguous run of the packed output
+// and each half a 36-real block per site; with a caller layout each warp
+// writes its sites' blocks one site at a time.
+template <typename T, int ISIGN, int HALF>
+__device__ __forceinline__ void force_half(const ForceArgs &a, int p, int h0, int h, const Nbr &n,
+                                           const cx<T> (&own)[4][3], T *stage) {
     using Q = typename VecOf<T>::S;  // 16-byte vector: float4 or double2
     constexpr int NS = ForceTile<T>::sites;
     constexpr int QPS = 72 * (int)sizeof(T) / 16;  // 16-byte vectors per site
-    __shared__ __align__(16) T stage[NS * 72];
-    const int p = blockIdx.y;
-    const int h0 = blockIdx.x * NS;
-    const int h = h0 + threadIdx.x;
+    constexpr int QH = QPS / 2;                    // per half
     if (h < a.g.Vh) {
-        Nbr n;
-        neighbours<4>(a.g, h, p, n);
-        cx<T> own[4][3];
-        F::load_spinor(static_cast<const V *>(p == a.pt ? a.chi : a.psi), a.g.stride, h, own);
-        T *st = stage + threadIdx.x * 72;
-        force_link<T, ISIGN, 0>(a, p, h, n, own, st);
-        force_link<T, ISIGN, 1>(a, p, h, n, own, st);
-        force_link<T, ISIGN, 2>(a, p, h, n, own, st);
-        force_link<T, ISIGN, 3>(a, p, h, n, own, st);
+        T *st = stage + threadIdx.x * 36;
+        force_link<T, ISIGN, 2 * HALF>(a, p, h, n, own, st);
+        force_link<T, ISIGN, 2 * HALF + 1>(a, p, h, n, own, st + 18);
     }
     __syncthreads();
     const int nsites = min(NS, a.g.Vh - h0);
     const Q *sq = reinterpret_cast<const Q *>(stage);
     Q *out = static_cast<Q *>(a.out);
     if (!a.table) {
-        Q *dst = out + (size_t)(p * a.g.Vh + h0) * QPS;
-        for (int i = threadIdx.x; i < nsites * QPS; i += NS) {
+        Q *dst = out + (size_t)(p * a.g.Vh + h0) * QPS + HALF * QH;
+        for (int i = threadIdx.x; i < nsites * QH; i += NS) {
+            const int s = i / QH, j = i - s * QH;
             Q v = sq[i];
+            Q *d = dst + (size_t)s * QPS + j;
             if (a.accumulate) {
-                const Q w = dst[i];
+                const Q w = *d;
                 if constexpr (sizeof(T) == 4) v = make_float4(w.x + v.x, w.y + v.y, w.z + v.z, w.w + v.w);
                 else v = make_double2(w.x + v.x, w.y + v.y);
             }
-            dst[i] = v;
+            *d = v;
         }
     } else {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         for (int k = w * 32; k < min(nsites, w * 32 + 32); k++) {
-            Q *dst = out + (size_t)a.table[p * a.g.Vh + h0 + k] * QPS;
-            for (int i = lane; i < QPS; i += 32) {
-                Q v = sq[k * QPS + i];
+            Q *dst = out + (size_t)a.table[p * a.g.Vh + h0 + k] * QPS + HALF * QH;
+            for (int i = lane; i < QH; i += 32) {
+                Q v = sq[k * QH + i];
                 if (a.accumulate) {
                     const Q w2 = dst[i];
                     if constexpr (sizeof(T) == 4) v = make_float4(w2.x + v.x, w2.y + v.y, w2.z + v.z, w2.w + v.w);
@@ -214,6 +209,26 @@ __global__ void __launch_bounds__(ForceTile<T>::sites) force_kernel(const ForceA
             }
         }
     }
+    __syncthreads();  // the staging area is refilled by the next half
+}
+
+template <typename T, int ISIGN>
+__global__ void __launch_bounds__(ForceTile<T>::sites, ForceTile<T>::min_blocks) force_kernel(const ForceArgs a) {
+    using F = Field<T>;
+    using V = typename VecOf<T>::S;
+    constexpr int NS = ForceTile<T>::sites;
+    __shared__ __align__(16) T stage[NS * 36];
+    const int p = blockIdx.y;
+    const int h0 = blockIdx.x * NS;
+    const int h = h0 + threadIdx.x;
+    Nbr n;
+    cx<T> own[4][3];
+    if (h < a.g.Vh) {
+        neighbours<4>(a.g, h, p, n);
+        F::load_spinor(static_cast<const V *>(p == a.pt ? a.chi : a.psi), a.g.stride, h, own);
+    }
+    force_half<T, ISIGN, 0>(a, p, h0, h, n, own, stage);
+    force_half<T, ISIGN, 1>(a, p, h0, h, n, own, stage);
 }
 
 }  // namespace
