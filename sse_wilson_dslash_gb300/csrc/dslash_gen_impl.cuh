@@ -2,6 +2,8 @@
 // instantiated per storage format by dslash_gen_f32.cu / dslash_gen_half.cu.
 #pragma once
 
+#include <atomic>
+
 #include "dslash_gen.cuh"
 
 namespace gbds {
@@ -117,14 +119,19 @@ void launch_gen4_nrhs(const GenArgs &a, int nrhs, cudaStream_t st) {
 }
 
 // Variant 4 (16-bit storage): dynamic shared memory above the 48 KB default,
-// allowed once per kernel instance before its first launch.
+// allowed once per kernel instance and device before its first launch there.
 template <int FMT, int RECON, int ISIGN, int NRHS>
 void launch_gen5_one(const GenArgs &a, cudaStream_t st) {
     using SM = G5Smem<FMT, NRHS>;
     auto k = dslash_gen5_kernel<FMT, RECON, ISIGN, NRHS>;
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::bytes);
-    if (attr != cudaSuccess) return;  // the error stays the runtime's last error
+    constexpr int kMaxDev = 64;
+    static std::atomic<bool> ready[kMaxDev];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;  // the error stays the runtime's last error
+    if (dev < 0 || dev >= kMaxDev || !ready[dev].load()) {
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::bytes) != cudaSuccess) return;
+        if (dev >= 0 && dev < kMaxDev) ready[dev].store(true);
+    }
     const unsigned vh = (unsigned)a.g.Vh;
     launch_pdl_smem(k, dim3((vh + SM::P - 1) / SM::P), 128, SM::bytes, st, a);
 }
