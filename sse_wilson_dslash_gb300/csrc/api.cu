@@ -126,11 +126,13 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     // storage); from 16 rhs on (at 24^3x48) 2 is fastest where it exists and
     // 1 for FP32 (autotune chooses per shape).
     const bool gen = nrhs > 1 || format != GBDS_SPINOR_NATIVE;
-    // from 16 rhs on: for bfloat16 the fully packed kernel with two rhs a
-    // thread and cp.async prefetching (variant 4), for half + norm and FP32
-    // pairs the same without prefetching (3), for FP32 the packed multiply (1)
-    const int gen_variant =
-        nrhs >= 16 ? (format == GBDS_SPINOR_BF16 ? 4 : (format != GBDS_SPINOR_NATIVE ? 3 : 1)) : 0;
+    // from 16 rhs on: for 16-bit storage the fully packed kernel with two rhs
+    // a thread and cp.async prefetching (variant 4), for FP32 pairs the same
+    // without prefetching (3), for FP32 the packed multiply (1)
+    const int gen_variant = nrhs >= 16 ? (format == GBDS_SPINOR_BF16 || format == GBDS_SPINOR_F16_NORM
+                                              ? 4
+                                              : (format == GBDS_SPINOR_F32_PAIRS ? 3 : 1))
+                                       : 0;
     o->variant = gen ? gen_variant : ((prec == 32 && recon == 18) ? 1 : 0);
     o->tensor_cores = 0;
     o->d_err = nullptr;

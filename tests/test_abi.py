@@ -92,10 +92,10 @@ def test_spinor_formats_and_their_variants(libs):
         assert L.gbds_op_spinor_bytes(h) == nbytes * st.value * 32
         assert L.gbds_op_num_variants(h) == nv
         # default from 16 rhs on: variant 4 (two rhs a thread, prefetched) for
-        # bfloat16, 3 (two rhs a thread) for half + norm and FP32 pairs, 1 for FP32
+        # the 16-bit formats, 3 (two rhs a thread) for FP32 pairs, 1 for FP32
         blk, var = ctypes.c_int(), ctypes.c_int()
         assert L.gbds_op_get_tuning(h, ctypes.byref(blk), ctypes.byref(var)) == 0
-        assert var.value == {0: 1, 1: 4, 2: 3, 3: 3}[fmt]
+        assert var.value == {0: 1, 1: 4, 2: 4, 3: 3}[fmt]
         if fmt in (0, 3):
             assert L.gbds_op_set_tensor_cores(h, 1) != 0
         L.gbds_op_destroy(h)
