@@ -846,9 +846,14 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <int FMT, int NRHS>
 struct G5Smem {
     static constexpr int P = 256 / NRHS;  // sites per 128-thread CTA (two rhs a thread)
+    // ring slots (hops prefetched SLOTS - 1 ahead) and the CTAs per SM the
+    // registers are capped for: two slots at 5 CTAs measured slower (BF16,
+    // 32 rhs, 24^3x48: 0.455 against 0.437 ms)
+    static constexpr int SLOTS = 3;
+    static constexpr int MINB = 4;
     static constexpr size_t link_bytes = (size_t)P * 8 * 9 * 16;
-    static constexpr size_t ring_bytes = (size_t)3 * 2 * 3 * 128 * 16;
-    static constexpr size_t norm_bytes = FMT == kFmtF16N ? (size_t)3 * 2 * 128 * 4 : 0;
+    static constexpr size_t ring_bytes = (size_t)SLOTS * 2 * 3 * 128 * 16;
+    static constexpr size_t norm_bytes = FMT == kFmtF16N ? (size_t)SLOTS * 2 * 128 * 4 : 0;
     static constexpr size_t bytes = link_bytes + ring_bytes + norm_bytes;
 };
 
@@ -893,7 +898,7 @@ __device__ __forceinline__ float g5_read(const uint4 *ring, const float *rnorm, 
 }
 
 template <int FMT, int RECON, int ISIGN, int NRHS>
-__global__ void __launch_bounds__(128, 4) dslash_gen5_kernel(const GenArgs a) {
+__global__ void __launch_bounds__(128, G5Smem<FMT, NRHS>::MINB) dslash_gen5_kernel(const GenArgs a) {
     static_assert(FMT == kFmtBF16 || FMT == kFmtF16N, "16-bit storage");
     static_assert(NRHS >= 8 && NRHS <= 32, "8 to 32 right-hand sides");
     pdl_allow_next();
@@ -912,11 +917,14 @@ __global__ void __launch_bounds__(128, 4) dslash_gen5_kernel(const GenArgs a) {
     const bool act = h < a.g.Vh;
     Nbr n;
     if (act) neighbours<4>(a.g, h, a.pt, n);
-    // hops 0 and 1 in flight during the link staging
+    constexpr int NS = SM::SLOTS, DIST = NS - 1;  // hop K + DIST is issued during hop K
+    // the first DIST hops in flight during the link staging
     if (act) g5_issue<FMT, NRHS, 0, 0>(a, n, r, ring, rnorm);
     cp_async_commit();
-    if (act) g5_issue<FMT, NRHS, 1, 1>(a, n, r, ring, rnorm);
-    cp_async_commit();
+    if constexpr (DIST > 1) {
+        if (act) g5_issue<FMT, NRHS, 1, 1>(a, n, r, ring, rnorm);
+        cp_async_commit();
+    }
     for (int l = r; act && l < 8; l += H) {
         const int mu = l >> 1;
         const bool bwd = l & 1;
@@ -944,18 +952,19 @@ __global__ void __launch_bounds__(128, 4) dslash_gen5_kernel(const GenArgs a) {
     for (int q = 0; q < 2; q++)
 #pragma unroll
         for (int c = 0; c < 3; c++) UR[q][c] = UI[q][c] = LR[q][c] = LI[q][c] = make_float2(0.f, 0.f);
-    // hop K = 2 mu + (0 forward, 1 backward) from slot K % 3; then slot
-    // (K + 2) % 3, read during hop K - 1, takes hop K + 2
+    // hop K = 2 mu + (0 forward, 1 backward) from slot K % NS; then slot
+    // (K + DIST) % NS, read during hop K - 1, takes hop K + DIST
 #define GBDS_G5_HOP(K, MU, LORD, SIG)                                                             \
     {                                                                                             \
-        cp_async_wait<1>();                                                                       \
+        cp_async_wait<DIST - 1>();                                                                \
         float2 R[2][3], I[2][3];                                                                  \
         _Pragma("unroll") for (int q = 0; q < 2; q++) {                                          \
             float v[24];                                                                          \
-            const float sc = g5_read<FMT, (K) % 3>(ring, rnorm, q, v);                            \
+            const float sc = g5_read<FMT, (K) % NS>(ring, rnorm, q, v);                           \
             packed_project<MU, SIG, SCALE>(v, sc, R[q], I[q]);                                    \
         }                                                                                         \
-        if constexpr ((K) + 2 < 8) g5_issue<FMT, NRHS, ((K) + 2) & 7, ((K) + 2) % 3>(a, n, r, ring, rnorm); \
+        if constexpr ((K) + DIST < 8)                                                             \
+            g5_issue<FMT, NRHS, ((K) + DIST) & 7, ((K) + DIST) % NS>(a, n, r, ring, rnorm);       \
         cp_async_commit();                                                                        \
         packed_mul_recon2<MU, SIG, LORD, true>(sL[p][K], R, I, UR, UI, LR, LI);                   \
     }
