@@ -228,3 +228,37 @@ print("ref", legacy.refcount(64, 4))
     assert r.returncode == 0, r.stderr
     assert r.stdout.count("ref 0") == 2
     assert "one-to-one" in r.stderr and "not the inverse" in r.stderr
+
+
+def test_split_t_entry_points_validate_before_any_device_work(libs):
+    """gbds_op_face_bytes / gbds_op_pack_faces / gbds_op_dslash_halo: face
+    size, unsupported operators, bad arguments and the silent isign no-op are
+    all decided on the host."""
+    from sse_wilson_dslash_gb300 import _lib
+    L = _lib.core()
+    vp = ctypes.c_void_p
+    h = vp()
+    d = (ctypes.c_int * 4)(8, 4, 6, 10)
+    assert L.gbds_op_create(ctypes.byref(h), d, 4, 32, 18) == 0
+    # one checkerboard of a time slice: 8 * 4 * 6 / 2 half spinors of 12 reals
+    assert L.gbds_op_face_bytes(h) == 96 * 12 * 4
+    a = vp(1 << 20)  # 16-byte aligned stand-ins: nothing below dereferences them
+    bad = vp((1 << 20) + 8)
+    assert L.gbds_op_pack_faces(h, a, a, 0, 0, a, a, None) == 0          # isign 0: no-op
+    assert L.gbds_op_pack_faces(h, a, a, 1, 2, a, a, None) == 1          # cb
+    assert L.gbds_op_pack_faces(h, a, a, 1, 0, None, a, None) == 1       # NULL face
+    assert L.gbds_op_pack_faces(h, a, a, 1, 0, bad, a, None) == 1        # misaligned
+    assert L.gbds_op_dslash_halo(h, a, a, a, a, a, 1, 0, 7, None) == 1   # part
+    assert L.gbds_op_dslash_halo(h, a, a, None, a, a, 1, 0, 0, None) == 1  # faces needed
+    assert L.gbds_op_dslash_halo(h, a, a, a, a, a, -2, 0, 0, None) == 0  # isign: no-op
+    L.gbds_op_destroy(h)
+    d64 = (ctypes.c_int * 4)(4, 4, 4, 4)
+    assert L.gbds_op_create(ctypes.byref(h), d64, 4, 64, 12) == 0
+    assert L.gbds_op_face_bytes(h) == 32 * 12 * 8
+    L.gbds_op_destroy(h)
+    # several rhs, another storage format or the 3D operator: not split
+    for nd, nrhs, fmt in ((4, 8, 0), (4, 1, 1), (3, 1, 0)):
+        assert L.gbds_op_create_ex(ctypes.byref(h), d64, nd, 32, 18, nrhs, fmt) == 0
+        assert L.gbds_op_pack_faces(h, a, a, 1, 0, a, a, None) == 5
+        assert L.gbds_op_dslash_halo(h, a, a, a, a, a, 1, 0, 0, None) == 5
+        L.gbds_op_destroy(h)
