@@ -58,6 +58,49 @@ __device__ __forceinline__ void outer_acc(cx<T> (&G)[3][3], const cx<T> (&a)[3],
         }
 }
 
+// F = TA(M), M = G U^+ with G = sum_s a_s (x) conj(b_s): M = sum_s a_s (x)
+// conj(U b_s), so two SU(3) matrix-vector products and two outer products
+// (144 real FMA) instead of G and then G U^+ (180): the FP64 kernel, which
+// is FP64-issue bound (16^4: 0.219 -> 0.165 ms).
+template <typename T>
+__device__ __forceinline__ void traceless_antihermitian_of_GUdag(const cx<T> (&a)[2][3], const cx<T> (&b)[2][3],
+                                                                 const cx<T> (&U)[3][3], cx<T> (&F)[3][3]) {
+    cx<T> c[2][3];  // c_s = U b_s
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            T re = 0, im = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                re = fma(U[j][k].r, b[s][k].r, re);
+                re = fma(-U[j][k].i, b[s][k].i, re);
+                im = fma(U[j][k].r, b[s][k].i, im);
+                im = fma(U[j][k].i, b[s][k].r, im);
+            }
+            c[s][j] = {re, im};
+        }
+    cx<T> M[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) M[i][j] = {T(0), T(0)};
+    outer_acc(M, a[0], c[0]);
+    outer_acc(M, a[1], c[1]);
+    const T tr_im = (M[0][0].i + M[1][1].i + M[2][2].i) / T(3);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            // (M - M^+)/2
+            F[i][j] = {(M[i][j].r - M[j][i].r) / T(2), (M[i][j].i + M[j][i].i) / T(2)};
+        }
+#pragma unroll
+    for (int i = 0; i < 3; i++) F[i][i].i -= tr_im;
+}
+
+// F = TA(G U^+) from G itself (the FP32 kernel, memory- and latency-bound,
+// measured faster in this form)
 template <typename T>
 __device__ __forceinline__ void traceless_antihermitian_of_GUdag(const cx<T> (&G)[3][3], const cx<T> (&U)[3][3],
                                                                  cx<T> (&F)[3][3]) {
@@ -78,10 +121,7 @@ __device__ __forceinline__ void traceless_antihermitian_of_GUdag(const cx<T> (&G
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-            // (M - M^+)/2
-            F[i][j] = {(M[i][j].r - M[j][i].r) / T(2), (M[i][j].i + M[j][i].i) / T(2)};
-        }
+        for (int j = 0; j < 3; j++) F[i][j] = {(M[i][j].r - M[j][i].r) / T(2), (M[i][j].i + M[j][i].i) / T(2)};
 #pragma unroll
     for (int i = 0; i < 3; i++) F[i][i].i -= tr_im;
 }
@@ -115,37 +155,42 @@ __device__ __forceinline__ void force_link(const ForceArgs &a, int p, int h, con
                                            T *o) {
     using F = Field<T>;
     using V = typename VecOf<T>::S;
-    cx<T> G[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) G[i][j] = {T(0), T(0)};
-    cx<T> s[4][3], hs[2][3], xi[2][3];
+    // G = sum_s ga_s (x) conj(gb_s)
+    cx<T> s[4][3], ga[2][3], gb[2][3];
     if (p == a.pt) {
         // forward hop at x: xi from chi(x) (own), half spinor of psi(x + mu)
-        fold<MU, ISIGN>(own, xi);
+        fold<MU, ISIGN>(own, ga);
         F::load_spinor(static_cast<const V *>(a.psi), a.g.stride, n.f[MU], s);
-        project<MU, ISIGN>(s, hs);
-        outer_acc(G, xi[0], hs[0]);
-        outer_acc(G, xi[1], hs[1]);
+        project<MU, ISIGN>(s, gb);
     } else {
         // backward hop into y = x + mu: half spinor of psi(x) (own), xi from chi(y)
-        project<MU, -ISIGN>(own, hs);
+        project<MU, -ISIGN>(own, ga);
         F::load_spinor(static_cast<const V *>(a.chi), a.g.stride, n.f[MU], s);
-        fold<MU, -ISIGN>(s, xi);
-        outer_acc(G, hs[0], xi[0]);
-        outer_acc(G, hs[1], xi[1]);
+        fold<MU, -ISIGN>(s, gb);
     }
     cx<T> R[3][3];
     if (a.mode == 1) {
         cx<T> U[3][3];
         F::template load_link<18>(a.gauge + (size_t)(p * 4 + MU) * a.link_block_bytes, a.g.stride, h, U);
-        traceless_antihermitian_of_GUdag(G, U, R);
+        if constexpr (sizeof(T) == 8) {
+            traceless_antihermitian_of_GUdag(ga, gb, U, R);
+        } else {
+            cx<T> G[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) G[i][j] = {T(0), T(0)};
+            outer_acc(G, ga[0], gb[0]);
+            outer_acc(G, ga[1], gb[1]);
+            traceless_antihermitian_of_GUdag(G, U, R);
+        }
     } else {
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int j = 0; j < 3; j++) R[i][j] = G[i][j];
+            for (int j = 0; j < 3; j++) R[i][j] = {T(0), T(0)};
+        outer_acc(R, ga[0], gb[0]);
+        outer_acc(R, ga[1], gb[1]);
     }
     const T c = (T)a.coef;
 #pragma unroll
