@@ -849,6 +849,7 @@ def run_profile_case(args):
             op.set_tensor_cores(True)
         elif args.variant >= 0:
             op.set_tuning(0, args.variant)
+        op.set_site_order(args.zblock)
         u = su3_links(V * 4, gen, torch).float().reshape(-1)
         psi = torch.randn(args.nrhs * V * 24, dtype=torch.float32, device="cuda", generator=gen)
     else:
@@ -879,7 +880,7 @@ def run_profile_case(args):
     torch.cuda.synchronize()
     op.check()
     print(json.dumps({"profile": kind, "dims": list(dims), "ms": e0.elapsed_time(e1) / args.steps,
-                      "tuning": list(op.tuning())}), flush=True)
+                      "tuning": list(op.tuning()), "zblock": op.site_order()}), flush=True)
     return 0
 
 
@@ -908,6 +909,8 @@ def main():
     ap.add_argument("--fmt", default="bf16", help="--profile multi_rhs: native, f32_pairs, bf16 or f16")
     ap.add_argument("--variant", type=int, default=-1, help="--profile: kernel variant (-1: the default)")
     ap.add_argument("--tc", action="store_true", help="--profile multi_rhs: the tensor-core kernel")
+    ap.add_argument("--zblock", type=int, default=-1,
+                    help="--profile multi_rhs: site order (z slab planes; 0 natural, -1 the default)")
     args = ap.parse_args()
     if args.dims:
         global DIMS, WORKLOAD

@@ -176,6 +176,19 @@ int gbds_op_set_tuning(gbds_op op, int threads, int variant);
 int gbds_op_get_tuning(gbds_op op, int *threads, int *variant);
 int gbds_op_num_variants(gbds_op op);
 
+/* Site order of the multi-RHS CUDA-core kernels (operators with several
+ * right-hand sides or 16-bit storage; the tensor-core kernel keeps its own
+ * tile order).  zblock = B, a divisor of the z extent: the lattice is swept
+ * in z slabs of B (z, t) planes, t outside z within each slab, so that a
+ * source spinor's eight reads stay within about 2 B planes and hit L2; 0 or
+ * Lz: the natural checkerboard order; -1: the default, the largest slab whose
+ * reuse span fits in a fixed share of L2 (natural order when the whole
+ * lattice's span fits).  Results are the same in every order up to the
+ * per-block partial sums' order.  Storage layouts do not change.
+ * get: the slab in use (0 = natural order). */
+int gbds_op_set_site_order(gbds_op op, int zblock);
+int gbds_op_get_site_order(gbds_op op, int *zblock);
+
 /* Time every (block, variant) candidate of gbds_op_dslash on the caller's
  * fields (res is overwritten), keep the fastest for this operator and cache
  * it process-wide for its (dims, nd, prec, recon, nrhs, format); a later call

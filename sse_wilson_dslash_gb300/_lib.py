@@ -80,6 +80,8 @@ def core() -> ctypes.CDLL:
     L.gbds_op_set_tuning.argtypes = [vp, i, i]
     L.gbds_op_num_variants.argtypes = [vp]
     L.gbds_op_get_tuning.argtypes = [vp, c_int_p, c_int_p]
+    L.gbds_op_set_site_order.argtypes = [vp, i]
+    L.gbds_op_get_site_order.argtypes = [vp, c_int_p]
     L.gbds_op_autotune.argtypes = [vp, vp, vp, vp, vp]
     L.gbds_op_pack_gauge.argtypes = [vp, vp, vp, vp]
     L.gbds_op_pack_spinor.argtypes = [vp, vp, i, vp, vp]

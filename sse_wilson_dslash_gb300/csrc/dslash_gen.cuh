@@ -236,6 +236,29 @@ struct GenArgs {
 template <int NRHS>
 __device__ __forceinline__ int nrhs_of(const GenArgs &a) { return NRHS > 0 ? NRHS : a.nrhs; }
 
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Site of logical index j in the multi-RHS kernels' traversal order.  With
+// g.zblock = B (a divisor of Lz below Lz) the lattice is swept in z slabs of
+// B (z, t) planes with t outside z inside each slab: (x, y) fastest, then z
+// within the slab, then t, then the slab.  A source spinor is then read by
+// CTAs at most ~2 B planes apart (2 Lz planes in the natural order), which
+// keeps its eight reads in L2 when a plane of all right-hand sides is large;
+// the planes next to a slab's z faces are read from DRAM twice.  B = 0: the
+// natural (cb2) order.
+__device__ __forceinline__ int gen_site(const Geom &g, int j) {
+    const int B = g.zblock;
+    if (B <= 0 || j >= g.Vh) return j;
+    const int plane = g.Lxh * g.L[1];
+    const int w = j % plane;
+    int q = j / plane;
+    const int zz = q % B;
+    q /= B;
+    const int t = q % g.L[3];
+    const int z = (q / g.L[3]) * B + zz;
+    return (t * g.L[2] + z) * plane + w;
+}
+
 template <int FMT, int RECON, int ISIGN, int NRHS, int MU, int LFMT>
 __device__ __forceinline__ void gen_hop_pair(const GenArgs &a, int h, int r, const Nbr &n, cx<float> (&acc)[4][3]) {
     const int ps = 1 - a.pt;
@@ -369,7 +392,7 @@ __global__ void __launch_bounds__(128, 6) dslash_gen2_kernel(const GenArgs a) {
     __shared__ float4 sL[P][8][9];
     const int t = threadIdx.x;
     const int p = t / NRHS, r = t % NRHS;
-    const int h = blockIdx.x * P + p;
+    const int h = gen_site(a.g, blockIdx.x * P + p);
     const bool act = h < a.g.Vh;
     Nbr n;
     if (act) neighbours<4>(a.g, h, a.pt, n);
@@ -565,8 +588,20 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
     __shared__ float4 sL[P][8][9];
     const int t = threadIdx.x;
     const int p = t / NRHS, r = t % NRHS;
-    const int h = blockIdx.x * P + p;
+    const int h = gen_site(a.g, blockIdx.x * P + p);
     const bool act = h < a.g.Vh;
+    if constexpr (EPI >= 2 && FMT == kFmtF32Pairs) {
+        // the epilogue's operands (x, and r for the CG update) toward L2 now:
+        // their loads come after the hops, at the end of the thread
+        if (act) {
+            const size_t i = (size_t)h * NRHS + r;
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                prefetch_l2(reinterpret_cast<const float4 *>(a.x) + (size_t)k * a.cs + i);
+                if constexpr (EPI == 3) prefetch_l2(a.rvec + (size_t)k * a.cs + i);
+            }
+        }
+    }
     Nbr n;
     if (act) neighbours<4>(a.g, h, a.pt, n);
     if (act && r < 8) {
@@ -750,7 +785,7 @@ __global__ void __launch_bounds__(128, 4) dslash_gen4_kernel(const GenArgs a) {
     __shared__ float4 sL[P][8][9];
     const int t = threadIdx.x;
     const int p = t / H, r = t % H;  // this thread: rhs r and r + H of site p
-    const int h = blockIdx.x * P + p;
+    const int h = gen_site(a.g, blockIdx.x * P + p);
     const bool act = h < a.g.Vh;
     Nbr n;
     if (act) neighbours<4>(a.g, h, a.pt, n);
@@ -913,7 +948,7 @@ __global__ void __launch_bounds__(128, G5Smem<FMT, NRHS>::MINB) dslash_gen5_kern
     float *rnorm = reinterpret_cast<float *>(g5s + SM::link_bytes + SM::ring_bytes);
     const int t = threadIdx.x;
     const int p = t / H, r = t % H;
-    const int h = blockIdx.x * P + p;
+    const int h = gen_site(a.g, blockIdx.x * P + p);
     const bool act = h < a.g.Vh;
     Nbr n;
     if (act) neighbours<4>(a.g, h, a.pt, n);
@@ -1008,7 +1043,8 @@ __global__ void __launch_bounds__(128, 6) dslash_gen_kernel(const GenArgs a) {
     pdl_wait_prev();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nr = nrhs_of<NRHS>(a);
-    const int h = t / nr, r = t - h * nr;
+    const int j = t / nr, r = t - j * nr;
+    const int h = gen_site(a.g, j);
     float nrm = 0.f;
     if (h < a.g.Vh) {
         Nbr n;

@@ -19,6 +19,8 @@ struct Geom {
     int V;        // full volume
     int Vh;       // sites per checkerboard
     int stride;   // elements between consecutive components of a field
+    int zblock;   // site order of the multi-RHS kernels: z slabs of this many
+                  // planes, t swept inside each (0: natural order; gen_site)
 };
 
 // Record an error message for gbds_get_last_error() and return `code`.
@@ -87,6 +89,9 @@ cudaError_t launch_gen_f32p_cg_update(const Geom &g, int recon, int nrhs, const 
                                       int cb, const void *x, float coef, const RhsCgScalars *rsc, void *r,
                                       double *partials, cudaStream_t st);
 inline int gen_spinor_bytes(int fmt) { return (fmt == 0 || fmt == 3) ? 96 : (fmt == 1 ? 48 : 52); }
+// z slab of the multi-RHS kernels' site order for nrhs right-hand sides in
+// format fmt with recon-real FP32 links (0: the natural order)
+int gen_zblock(const Geom &g, int nrhs, int fmt, int recon);
 // Tensor-core form (dslash_tc.cu): fmt 1 / 2, nrhs 16 or 32, FP32 links
 // converted to the 16-bit operand type; err set to 1 on a timed-out wait.
 cudaError_t launch_gen_tc(int fmt, const Geom &g, int recon, int nrhs, const void *gauge, const void *psi, void *res,

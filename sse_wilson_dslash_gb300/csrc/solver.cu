@@ -1037,40 +1037,76 @@ __global__ void __launch_bounds__(128) bscale_copy(const float4 *__restrict__ v,
     }
 }
 
-// columns q of the multi-RHS inner fields: r = p = r64 / |r64|
-__global__ void __launch_bounds__(128) bdemote(const double2 *__restrict__ r64, double inv, float4 *r, float4 *p,
-                                              int Vh, int stride, int nrhs, int q, size_t cs) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= Vh) return;
-    // the inner fields are FP32 spin pairs: float4 k holds complex elements
-    // e0 and e0 + 3 (spins 0/1 or 2/3 of colour k % 3) as (e0.r, e1.r, e0.i,
-    // e1.i)
-#pragma unroll
+// The per-rhs FP64 fields of all rhs and a scale for each, in the kernel
+// parameters (512 bytes).
+struct RhsFields {
+    double2 *v[32];
+    double s[32];
+};
+
+// All columns of the multi-RHS inner fields in one launch.  A CTA of 256
+// threads takes 32 sites: lane = site (coalesced reads of the per-rhs FP64
+// fields), warp w the rhs w, w + 8, ...
+constexpr int kBXSites = 32;
+
+// r = p = s_q r64_q (s_q = 1 / |r64_q|), or 0 where s_q = 0; each component
+// passes through a [site][rhs] tile in shared memory, so that the
+// interleaved (site, rhs) stores are contiguous too
+__global__ void __launch_bounds__(256) bdemote_all(const RhsFields f, float4 *r, float4 *p, int Vh, int stride,
+                                                  int nrhs, size_t cs) {
+    __shared__ float4 tile[kBXSites][33];  // padded: lanes of one rhs hit different banks
+    const int base = blockIdx.x * kBXSites;
+    const int h = base + (threadIdx.x & 31);
+    const int n = min(kBXSites, Vh - base) * nrhs;  // (site, rhs) entries of this CTA
+#pragma unroll 1
     for (int k = 0; k < 6; k++) {
+        // the inner fields are FP32 spin pairs: float4 k holds complex
+        // elements e0 and e0 + 3 (spins 0/1 or 2/3 of colour k % 3) as (e0.r,
+        // e1.r, e0.i, e1.i)
         const int e0 = (k < 3 ? 0 : 6) + k % 3;
-        const double2 a = r64[(size_t)e0 * stride + h], b = r64[(size_t)(e0 + 3) * stride + h];
-        const float4 f = make_float4((float)(a.x * inv), (float)(b.x * inv), (float)(a.y * inv), (float)(b.y * inv));
-        const size_t i = (size_t)k * cs + (size_t)h * nrhs + q;
-        r[i] = f;
-        p[i] = f;
+        if (h < Vh) {
+            for (int q = threadIdx.x >> 5; q < nrhs; q += 8) {
+                const double inv = f.s[q];
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (inv != 0.0) {
+                    const double2 *r64 = f.v[q];
+                    const double2 a = r64[(size_t)e0 * stride + h], b = r64[(size_t)(e0 + 3) * stride + h];
+                    v = make_float4((float)(a.x * inv), (float)(b.x * inv), (float)(a.y * inv), (float)(b.y * inv));
+                }
+                tile[threadIdx.x & 31][q] = v;
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const float4 v = tile[j / nrhs][j % nrhs];
+            const size_t i = (size_t)k * cs + (size_t)base * nrhs + j;
+            r[i] = v;
+            p[i] = v;
+        }
+        __syncthreads();
     }
 }
 
-// x64 += s * column q of e
-__global__ void __launch_bounds__(128) bpromote(const float4 *__restrict__ e, double s, double2 *x64, int Vh, int stride,
-                                               int nrhs, int q, size_t cs) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+// x64_q += s_q * column q of e for the rhs with s_q != 0
+__global__ void __launch_bounds__(256) bpromote_all(const float4 *__restrict__ e, const RhsFields f, int Vh, int stride,
+                                                   int nrhs, size_t cs) {
+    const int h = blockIdx.x * kBXSites + (threadIdx.x & 31);
     if (h >= Vh) return;
+    for (int q = threadIdx.x >> 5; q < nrhs; q += 8) {
+        const double s = f.s[q];
+        if (s == 0.0) continue;
+        double2 *x64 = f.v[q];
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-        const int e0 = (k < 3 ? 0 : 6) + k % 3;  // the pair layout, as in bdemote
-        const float4 v = e[(size_t)k * cs + (size_t)h * nrhs + q];
-        double2 &a = x64[(size_t)e0 * stride + h];
-        double2 &b = x64[(size_t)(e0 + 3) * stride + h];
-        a.x = fma(s, (double)v.x, a.x);
-        a.y = fma(s, (double)v.z, a.y);
-        b.x = fma(s, (double)v.y, b.x);
-        b.y = fma(s, (double)v.w, b.y);
+        for (int k = 0; k < 6; k++) {
+            const int e0 = (k < 3 ? 0 : 6) + k % 3;  // the pair layout, as in bdemote_all
+            const float4 v = e[(size_t)k * cs + (size_t)h * nrhs + q];
+            double2 &a = x64[(size_t)e0 * stride + h];
+            double2 &b = x64[(size_t)(e0 + 3) * stride + h];
+            a.x = fma(s, (double)v.x, a.x);
+            a.y = fma(s, (double)v.z, a.y);
+            b.x = fma(s, (double)v.y, b.x);
+            b.y = fma(s, (double)v.w, b.y);
+        }
     }
 }
 
@@ -1079,6 +1115,7 @@ __global__ void __launch_bounds__(128) bpromote(const float4 *__restrict__ e, do
 
 struct gbds_bsolver_s {
     gbds_solver s1 = nullptr;  // FP64 gauge, FP64 operator temporaries, FP32 links, reductions
+    Geom gm{};                 // s1's geometry with the multi-RHS kernels' site order
     int nrhs = 0;
     std::vector<void *> b64, x64, r64;  // per rhs, FP64, checkerboard 0
     void *e = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *Mp = nullptr, *t = nullptr;  // multi-RHS FP32
@@ -1115,12 +1152,13 @@ cudaError_t apply_Mb(gbds_bsolver b, const void *in, void *out, int isign, doubl
     gbds_solver s = b->s1;
     const float k2 = (float)(s->prm.kappa * s->prm.kappa);
     // inner fields in FP32 spin pairs: the fully packed FP32x2 kernel from 16
-    // rhs on (measured faster there)
+    // rhs on (measured faster there), two rhs a thread where there is no
+    // epilogue
     const int v = b->nrhs >= 16 ? 2 : 0;
-    cudaError_t e =
-        launch_gen_f32p(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, isign, 0, nullptr, 0.f, nullptr, st, v);
+    cudaError_t e = launch_gen_f32p(b->gm, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, isign, 0, nullptr, 0.f,
+                                    nullptr, st, v ? 3 : 0);
     if (e != cudaSuccess) return e;
-    return launch_gen_f32p(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, out, isign, 1, in, -k2, partials, st, v);
+    return launch_gen_f32p(b->gm, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, out, isign, 1, in, -k2, partials, st, v);
 }
 
 // The fully packed operator (16, 32 rhs) fuses the CG's r -= alpha Ap into
@@ -1132,9 +1170,9 @@ cudaError_t apply_Mb_dagger_update(gbds_bsolver b, const void *in, cudaStream_t 
     gbds_solver s = b->s1;
     const float k2 = (float)(s->prm.kappa * s->prm.kappa);
     cudaError_t e =
-        launch_gen_f32p(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, -1, 0, nullptr, 0.f, nullptr, st, 2);
+        launch_gen_f32p(b->gm, s->prm.inner_recon, b->nrhs, s->gauge32, in, b->t, -1, 0, nullptr, 0.f, nullptr, st, 3);
     if (e != cudaSuccess) return e;
-    return launch_gen_f32p_cg_update(s->g, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, -1, 1, in, -k2, b->bsc, b->r,
+    return launch_gen_f32p_cg_update(b->gm, s->prm.inner_recon, b->nrhs, s->gauge32, b->t, -1, 1, in, -k2, b->bsc, b->r,
                                      b->bpartials, st);
 }
 
@@ -1239,6 +1277,8 @@ extern "C" int gbds_bsolver_create(gbds_bsolver *out, const int dims[4], int nrh
         return rc;
     }
     const Geom &g = b->s1->g;
+    b->gm = g;
+    b->gm.zblock = gen_zblock(g, nrhs, GBDS_SPINOR_F32_PAIRS, p->inner_recon);
     const size_t f64 = spinor_bytes(g, 64), f32m = spinor_bytes(g, 32) * nrhs;
     cudaError_t e = cudaSuccess;
     for (auto *v : {&b->b64, &b->x64, &b->r64}) {
@@ -1311,12 +1351,14 @@ extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double
     bool first = true;
     while (e == cudaSuccess) {
         // c_q = M^+ (r_q / |r_q|) in FP32 for all right-hand sides at once, and |c_q|^2
-        e = cudaMemsetAsync(b->r, 0, spinor_bytes(g, 32) * nr, st);
-        for (int q = 0; q < nr && e == cudaSuccess; q++) {
-            if (!live[q]) continue;
-            bdemote<<<nb1, 128, 0, st>>>(static_cast<const double2 *>(b->r64[q]), 1.0 / std::sqrt(r2[q]),
-                                         static_cast<float4 *>(b->r), static_cast<float4 *>(b->p), g.Vh, g.stride, nr, q,
-                                         cs);
+        {
+            RhsFields f{};
+            for (int q = 0; q < nr; q++) {
+                f.v[q] = static_cast<double2 *>(b->r64[q]);
+                f.s[q] = live[q] ? 1.0 / std::sqrt(r2[q]) : 0.0;
+            }
+            bdemote_all<<<(g.Vh + kBXSites - 1) / kBXSites, 256, 0, st>>>(
+                f, static_cast<float4 *>(b->r), static_cast<float4 *>(b->p), g.Vh, g.stride, nr, cs);
             count_launch();
             e = cudaGetLastError();
         }
@@ -1380,14 +1422,21 @@ extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double
             most = std::max(most, it[q]);
         }
         total += most;
-        // x_q += |c_q| e_q;  r_q = b_q - M x_q in FP64
-        for (int q = 0; q < nr && e == cudaSuccess; q++) {
-            if (target[q] == 0.0) continue;
-            bpromote<<<nb1, 128, 0, st>>>(static_cast<const float4 *>(b->e), std::sqrt(n2[q]),
-                                          static_cast<double2 *>(b->x64[q]), g.Vh, g.stride, nr, q, cs);
+        // x_q += |c_q| e_q (all rhs in one launch);  r_q = b_q - M x_q in FP64
+        {
+            RhsFields f{};
+            for (int q = 0; q < nr; q++) {
+                f.v[q] = static_cast<double2 *>(b->x64[q]);
+                f.s[q] = target[q] == 0.0 ? 0.0 : std::sqrt(n2[q]);
+            }
+            bpromote_all<<<(g.Vh + kBXSites - 1) / kBXSites, 256, 0, st>>>(static_cast<const float4 *>(b->e), f, g.Vh,
+                                                                           g.stride, nr, cs);
             count_launch();
             e = cudaGetLastError();
-            if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, b->x64[q], s->t64, s->Mp64, +1, nullptr, st);
+        }
+        for (int q = 0; q < nr && e == cudaSuccess; q++) {
+            if (target[q] == 0.0) continue;
+            e = apply_M<double>(s, s->gauge64, 18, b->x64[q], s->t64, s->Mp64, +1, nullptr, st);
             if (e == cudaSuccess) {
                 xmy_norm<<<nb1, kThreads, 0, st>>>(static_cast<const double2 *>(b->b64[q]),
                                                    static_cast<const double2 *>(s->Mp64), static_cast<double2 *>(b->r64[q]),

@@ -98,6 +98,16 @@ class DslashOperator:
         _lib.check(_lib.core().gbds_op_get_tuning(self._h, ctypes.byref(b), ctypes.byref(v)))
         return b.value, v.value
 
+    def set_site_order(self, zblock: int) -> None:
+        """Site order of the multi-RHS kernels: z slabs of ``zblock`` planes
+        (a divisor of Lz), 0 the natural order, -1 the default."""
+        _lib.check(_lib.core().gbds_op_set_site_order(self._h, int(zblock)))
+
+    def site_order(self) -> int:
+        z = ctypes.c_int()
+        _lib.check(_lib.core().gbds_op_get_site_order(self._h, ctypes.byref(z)))
+        return z.value
+
     def autotune(self, gauge, psi, scratch, stream=None):
         """Pick the fastest launch configuration on these fields (scratch is overwritten)."""
         _lib.check(_lib.core().gbds_op_autotune(self._h, ctypes.c_void_p(_dptr(gauge)), ctypes.c_void_p(_dptr(psi)),

@@ -262,3 +262,42 @@ def test_split_t_entry_points_validate_before_any_device_work(libs):
         assert L.gbds_op_pack_faces(h, a, a, 1, 0, a, a, None) == 5
         assert L.gbds_op_dslash_halo(h, a, a, a, a, a, 1, 0, 0, None) == 5
         L.gbds_op_destroy(h)
+
+
+def test_site_order_validation_and_defaults(libs):
+    """gbds_op_set_site_order / gbds_op_get_site_order: divisors of Lz only,
+    Lz itself is the natural order, single-rhs operators keep the natural
+    order; the default slab is the largest divisor B of Lz whose 2 B planes
+    of traffic (nrhs source and target spinors and 8 links a site) fit in
+    64 MB, or the natural order when 2 Lz planes fit."""
+    from sse_wilson_dslash_gb300 import _lib
+    L = _lib.core()
+    h = ctypes.c_void_p()
+    z = ctypes.c_int()
+
+    def create(dims, nrhs, fmt, recon=18):
+        assert L.gbds_op_create_ex(ctypes.byref(h), (ctypes.c_int * 4)(*dims), 4, 32, recon, nrhs, fmt) == 0
+
+    def order():
+        assert L.gbds_op_get_site_order(h, ctypes.byref(z)) == 0
+        return z.value
+
+    create((8, 4, 6, 10), 16, 3)
+    assert order() == 0
+    for zb, rc, want in ((3, 0, 3), (6, 0, 0), (1, 0, 1), (4, 1, 1), (7, 1, 1), (-2, 1, 1), (2, 0, 2), (-1, 0, 0)):
+        assert L.gbds_op_set_site_order(h, zb) == rc, zb
+        assert order() == want, zb
+    L.gbds_op_destroy(h)
+    create((8, 4, 6, 10), 1, 0)
+    assert L.gbds_op_set_site_order(h, 2) == 5
+    assert L.gbds_op_set_site_order(h, 0) == 0 and L.gbds_op_set_site_order(h, -1) == 0 and order() == 0
+    L.gbds_op_destroy(h)
+    # 32^3x64, 16 rhs, FP32 pairs, recon 12: 512-site planes of 16 * 192 + 8 * 48 bytes a site
+    create((32, 32, 32, 64), 16, 3, recon=12)
+    assert order() == 16
+    L.gbds_op_destroy(h)
+    for nrhs, fmt, want in ((16, 3, 0), (32, 3, 12), (32, 0, 12), (32, 1, 0), (8, 0, 0)):
+        create((24, 24, 24, 48), nrhs, fmt)
+        assert order() == want, (nrhs, fmt)
+        L.gbds_op_destroy(h)
+

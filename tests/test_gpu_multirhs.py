@@ -233,7 +233,7 @@ def production():
     return dict(u=u, psi=psi, refs=refs, ts=torch.from_numpy(ts).cuda(), V=V)
 
 
-def _production_error(production, nrhs, fmt, variant=None, tc=False):
+def _production_error(production, nrhs, fmt, variant=None, tc=False, zblock=-1):
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
     P = production
@@ -242,6 +242,7 @@ def _production_error(production, nrhs, fmt, variant=None, tc=False):
         op.set_tensor_cores(True)
     elif variant is not None:
         op.set_tuning(0, variant)
+    op.set_site_order(zblock)
     gauge = op.pack_gauge(P["u"])
     out = op.apply(gauge, op.pack_spinor(P["psi"][:nrhs].reshape(-1), PROD_CB), PROD_ISIGN, PROD_CB)
     op.check()
@@ -336,3 +337,56 @@ def test_packed_variants_partial_last_cta(nrhs, fmt):
                 ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb)
                 assert O.site_rel_err(got[r], ref, ts) <= TOL[fmt], (variant, isign, cb, r)
         op.close()
+
+
+@pytest.mark.parametrize("fmt,nrhs", [("native", 4), ("native", 16), ("f32_pairs", 16), ("bf16", 32), ("f16", 8)])
+def test_site_orders_match_oracle(fmt, nrhs):
+    """The z-slab site orders of gbds_op_set_site_order against the natural
+    order (bit-identical outputs: every site runs the same arithmetic in any
+    order) and the oracle, for every CUDA-core variant: 6x2x6x10 has planes of
+    6 sites, so CTAs straddle planes and slabs; slabs of 1, 2 and 3 planes."""
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    dims = (6, 2, 6, 10)
+    V = O.volume(dims)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    rng = np.random.default_rng(700 + nrhs)
+    u = O.random_gauge(rng, V)
+    psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
+    isign, cb = -1, 1
+    ts = O.target_sites(4, dims, lol, cb)
+    refs = [O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb) for r in range(nrhs)]
+    variants = (0, 1) if fmt == "native" else (0, 1, 2, 3, 4)
+    for variant in variants:
+        op = DslashOperator(dims, nd=4, prec=32, recon=12, nrhs=nrhs, spinor_format=fmt)
+        op.set_tuning(0, variant)
+        gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
+        src = op.pack_spinor(torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda(), cb)
+        op.set_site_order(0)
+        assert op.site_order() == 0
+        natural = op.new_spinor().zero_()
+        op.apply(gauge, src, isign, cb, out=natural)
+        for zb in (1, 2, 3):
+            op.set_site_order(zb)
+            assert op.site_order() == zb
+            out = op.new_spinor().zero_()
+            op.apply(gauge, src, isign, cb, out=out)
+            torch.cuda.synchronize()
+            assert torch.equal(out, natural), (variant, zb)
+        res = torch.zeros(nrhs * V * 24, dtype=torch.float32, device="cuda")
+        op.unpack_spinor(natural, 1 - cb, res)
+        got = res.cpu().numpy().reshape(nrhs, V, 24)
+        for r in range(nrhs):
+            assert O.site_rel_err(got[r], refs[r], ts) <= TOL[fmt], (variant, r)
+        op.close()
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("fmt,nrhs,variant,zblock", [("bf16", 32, 4, 4), ("f16", 16, 3, 3), ("native", 32, 1, 2),
+                                                     ("f32_pairs", 16, 2, 6)])
+def test_site_order_24x24x24x48_every_rhs_against_oracle(production, fmt, nrhs, variant, zblock):
+    """Slabs chosen by hand at the configured size, every rhs and target site
+    against the oracle (the defaults' slabs are covered by the tests above)."""
+    err = _production_error(production, nrhs, fmt, variant=variant, zblock=zblock)
+    assert err <= TOL[fmt], (nrhs, fmt, variant, zblock, err)
+
