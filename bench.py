@@ -854,7 +854,8 @@ def run_profile_case(args):
         psi = torch.randn(args.nrhs * V * 24, dtype=torch.float32, device="cuda", generator=gen)
     else:
         dt = torch.float32 if args.prec == 32 else torch.float64
-        op = DslashOperator(dims, nd=4, prec=args.prec, recon=args.recon if kind == "dslash" else 18)
+        fmt = "double_float" if (kind == "dslash" and args.fmt == "double_float") else "native"
+        op = DslashOperator(dims, nd=4, prec=args.prec, recon=args.recon if kind == "dslash" else 18, spinor_format=fmt)
         if kind == "dslash" and args.variant >= 0:
             op.set_tuning(0, args.variant)
         u = su3_links(V * 4, gen, torch).to(dt).reshape(-1)
@@ -906,7 +907,8 @@ def main():
     ap.add_argument("--prec", type=int, default=32, help="--profile dslash/force: 32 or 64")
     ap.add_argument("--recon", type=int, default=18, help="--profile dslash/multi_rhs: 18 or 12")
     ap.add_argument("--nrhs", type=int, default=32, help="--profile multi_rhs: right-hand sides")
-    ap.add_argument("--fmt", default="bf16", help="--profile multi_rhs: native, f32_pairs, bf16 or f16")
+    ap.add_argument("--fmt", default="bf16",
+                    help="--profile multi_rhs: native, f32_pairs, bf16 or f16; --profile dslash --prec 64: double_float")
     ap.add_argument("--variant", type=int, default=-1, help="--profile: kernel variant (-1: the default)")
     ap.add_argument("--tc", action="store_true", help="--profile multi_rhs: the tensor-core kernel")
     ap.add_argument("--zblock", type=int, default=-1,

@@ -94,10 +94,23 @@ int gbds_op_destroy(gbds_op op);
                                   * (0..2) = (s0c.r, s1c.r, s0c.i, s1c.i), 3 + c =
                                   * (s2c.r, s3c.r, s2c.i, s3c.i); the operand
                                   * layout of the fully packed kernel (variant 2) */
+#define GBDS_SPINOR_DOUBLE_FLOAT 4 /* prec 64, one rhs: every double of the
+                                    * spinor and gauge fields held as an
+                                    * unevaluated FP32 sum hi + lo (48 of its
+                                    * 53 significant bits, FP32 exponent
+                                    * range), each complex one 16-byte
+                                    * (re.hi, re.lo, im.hi, im.lo) unit in
+                                    * the FP64 layout's place; the operator
+                                    * runs in double-float arithmetic on the
+                                    * FP32 pipes.  pack/unpack take and give
+                                    * FP64 arrays. */
 
 /* As gbds_op_create, for nrhs right-hand sides per site (1..32; powers of two
- * have specialised kernels) and a spinor storage format.  nrhs > 1 or a format
- * other than GBDS_SPINOR_NATIVE needs prec 32 and nd 4; arithmetic is FP32.  A field then holds nrhs spinors per
+ * have specialised kernels) and a spinor storage format.
+ * GBDS_SPINOR_DOUBLE_FLOAT needs prec 64 and nrhs 1 (nd 3 or 4; fields of
+ * FP64 size; not for the force or the split-t entry points).  nrhs > 1 or
+ * another format other than GBDS_SPINOR_NATIVE needs prec 32 and nd 4;
+ * arithmetic is FP32.  A field then holds nrhs spinors per
  * site, element (k, h, r) at k*stride*nrhs + h*nrhs + r (k: 16-byte component,
  * h: site, r: right-hand side), half formats followed by one float norm per
  * (h, r).  pack/unpack take FP32 packed arrays [nrhs][V][4][3][2]; the gauge

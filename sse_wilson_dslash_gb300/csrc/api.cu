@@ -123,9 +123,11 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     if (recon != 18 && recon != 12) return set_error(GBDS_ERROR_INVALID_VALUE, "recon must be 18 or 12");
     if (nrhs < 1 || nrhs > 32) return set_error(GBDS_ERROR_INVALID_VALUE, "nrhs must be in [1, 32]");
     if (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_BF16 && format != GBDS_SPINOR_F16_NORM &&
-        format != GBDS_SPINOR_F32_PAIRS)
+        format != GBDS_SPINOR_F32_PAIRS && format != GBDS_SPINOR_DOUBLE_FLOAT)
         return set_error(GBDS_ERROR_INVALID_VALUE, "unknown spinor format");
-    if ((nrhs > 1 || format != GBDS_SPINOR_NATIVE) && (prec != 32 || nd != 4))
+    if (format == GBDS_SPINOR_DOUBLE_FLOAT && (prec != 64 || nrhs != 1))
+        return set_error(GBDS_ERROR_UNSUPPORTED, "the double-float format needs prec 64 and one right-hand side");
+    if ((nrhs > 1 || (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_DOUBLE_FLOAT)) && (prec != 32 || nd != 4))
         return set_error(GBDS_ERROR_UNSUPPORTED,
                          "several right-hand sides and the non-native spinor formats need prec 32 and nd 4");
     Geom g;
@@ -148,7 +150,7 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     // FP32x2 colour multiply, 2 = the whole hop packed (16-bit and FP32-pair
     // storage); from 16 rhs on (at 24^3x48) 2 is fastest where it exists and
     // 1 for FP32 (autotune chooses per shape).
-    const bool gen = nrhs > 1 || format != GBDS_SPINOR_NATIVE;
+    const bool gen = nrhs > 1 || (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_DOUBLE_FLOAT);
     // from 16 rhs on: for 16-bit storage the fully packed kernel with two rhs
     // a thread and cp.async prefetching (variant 4), for FP32 pairs the same
     // without prefetching (3), for FP32 the packed multiply (1)
@@ -203,7 +205,11 @@ extern "C" int gbds_op_set_layout(gbds_op op, const int *site_table, int n) {
 
 extern "C" int gbds_op_is_canonical(gbds_op op) { return op && op->d_site_table == nullptr; }
 
-static bool generic(gbds_op op) { return op->nrhs > 1 || op->format != GBDS_SPINOR_NATIVE; }
+// the multi-RHS / reduced-storage kernels (FP32 arithmetic)
+static bool generic(gbds_op op) {
+    return op->nrhs > 1 || (op->format != GBDS_SPINOR_NATIVE && op->format != GBDS_SPINOR_DOUBLE_FLOAT);
+}
+static bool double_float(gbds_op op) { return op->format == GBDS_SPINOR_DOUBLE_FLOAT; }
 
 extern "C" size_t gbds_op_spinor_bytes(gbds_op op) {
     if (!op) return 0;
@@ -305,8 +311,8 @@ extern "C" int gbds_op_num_variants(gbds_op op) {
     if (!op) return 0;
     // 2: the fully packed kernel; 3: the same, two rhs a thread; 4: 3 with
     // cp.async prefetching (16-bit storage)
-    if (op->format != GBDS_SPINOR_NATIVE) return 5;
-    return op->nrhs > 1 ? 2 : dslash_variants(op->prec);
+    if (generic(op)) return op->format != GBDS_SPINOR_NATIVE ? 5 : 2;
+    return double_float(op) ? dslash_variants_df() : dslash_variants(op->prec);
 }
 
 namespace {
@@ -407,8 +413,10 @@ extern "C" int gbds_op_pack_gauge(gbds_op op, const void *u_packed, void *gauge,
     if (!aligned16(gauge)) return set_error(GBDS_ERROR_INVALID_VALUE, "gauge must be 16-byte aligned");
     if (reinterpret_cast<uintptr_t>(u_packed) & 7u)
         return set_error(GBDS_ERROR_INVALID_VALUE, "u_packed must be 8-byte aligned");
-    cudaError_t e = launch_pack_gauge(op->g, op->prec, op->recon, u_packed, op->d_site_table, gauge,
-                                      static_cast<cudaStream_t>(stream));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_pack_gauge(op->g, op->prec, op->recon, u_packed, op->d_site_table, gauge, st);
+    // double-float: the packed FP64 field converted in place, 16 bytes a complex
+    if (e == cudaSuccess && double_float(op)) e = launch_f64_to_df(gauge, gauge, gbds_op_gauge_bytes(op) / 16, st);
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_gauge");
 }
 
@@ -428,7 +436,8 @@ extern "C" int gbds_op_pack_spinor(gbds_op op, const void *psi_packed, int parit
                       : launch_pack_gen_half(op->format, op->g, op->nrhs, src, op->d_site_table, parity, spinor, st);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_spinor");
     }
-    cudaError_t e = launch_pack_spinor(op->g, op->prec, psi_packed, op->d_site_table, 0, parity, spinor, st);
+    cudaError_t e =
+        launch_pack_spinor(op->g, op->prec, psi_packed, op->d_site_table, 0, parity, spinor, st, double_float(op));
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "pack_spinor");
 }
 
@@ -448,7 +457,8 @@ extern "C" int gbds_op_unpack_spinor(gbds_op op, const void *spinor, int parity,
                       : launch_unpack_gen_half(op->format, op->g, op->nrhs, spinor, op->d_site_table, parity, dst, st);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "unpack_spinor");
     }
-    cudaError_t e = launch_unpack_spinor(op->g, op->prec, spinor, op->d_site_table, 0, parity, psi_packed, st);
+    cudaError_t e =
+        launch_unpack_spinor(op->g, op->prec, spinor, op->d_site_table, 0, parity, psi_packed, st, double_float(op));
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "unpack_spinor");
 }
 
@@ -477,8 +487,11 @@ extern "C" int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, vo
                                         nullptr, s, op->variant);
         return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
     }
-    cudaError_t e = op->prec == 32 ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)
-                                   : launch_dslash_f64(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s);
+    cudaError_t e =
+        op->prec == 32
+            ? launch_dslash_f32(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)
+            : (double_float(op) ? launch_dslash_df(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s)
+                                : launch_dslash_f64(op->g, op->recon, gauge, psi, res, isign, cb, op->block, op->variant, s));
     return e == cudaSuccess ? GBDS_SUCCESS : cuda_error(e, "dslash");
 }
 

@@ -13,6 +13,9 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
+#include "dfloat.cuh"
 #include "gbds_internal.h"
 
 namespace gbds {
@@ -79,7 +82,7 @@ __device__ __forceinline__ void su3_mul(const cx<T> (&U)[3][3], const cx<T> (&h)
     for (int k = 0; k < 2; k++) {
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            T re = 0, im = 0;
+            T re = T(0), im = T(0);
 #pragma unroll
             for (int j = 0; j < 3; j++) {
                 const cx<T> m = DAG ? U[j][i] : U[i][j];
@@ -251,9 +254,54 @@ struct Field<double> {
     }
 };
 
+// Double-float (dfloat.cuh): the FP64 layout with each double2 (one complex)
+// as a float4 (re.hi, re.lo, im.hi, im.lo).
+template <>
+struct Field<dfloat> {
+    static constexpr int SPINOR_VECS = 12;  // float4
+    __device__ __forceinline__ static void load_spinor(const float4 *__restrict__ p, int stride, int h,
+                                                       cx<dfloat> (&s)[4][3]) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+            const float4 q = __ldg(p + k * stride + h);
+            s[k / 3][k % 3] = {dfloat(q.x, q.y), dfloat(q.z, q.w)};
+        }
+    }
+    __device__ __forceinline__ static void store_spinor(float4 *__restrict__ p, int stride, int h,
+                                                        const cx<dfloat> (&s)[4][3]) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+            const cx<dfloat> &v = s[k / 3][k % 3];
+            __stcs(p + k * stride + h, make_float4(v.r.hi, v.r.lo, v.i.hi, v.i.lo));
+        }
+    }
+    static constexpr int link_vecs(int recon) { return recon == 18 ? 9 : 6; }
+    template <int RECON, bool ONCE = false>
+    __device__ __forceinline__ static void load_link(const void *__restrict__ base, int stride, int h,
+                                                     cx<dfloat> (&U)[3][3]) {
+        const uint64_t pol = ONCE ? l2_evict_first_policy() : 0;
+        const float4 *p = static_cast<const float4 *>(base);
+        constexpr int n = RECON == 18 ? 9 : 6;
+#pragma unroll
+        for (int k = 0; k < n; k++) {
+            const float4 q = ONCE ? ld_once(p + k * stride + h, pol) : __ldg(p + k * stride + h);
+            U[k / 3][k % 3] = {dfloat(q.x, q.y), dfloat(q.z, q.w)};
+        }
+        if constexpr (RECON == 12) reconstruct_row2(U);
+    }
+};
+
 template <typename T> struct VecOf;
 template <> struct VecOf<float> { using S = float4; using G = float2; static constexpr int GB = 8; };
 template <> struct VecOf<double> { using S = double2; using G = double2; static constexpr int GB = 16; };
+template <> struct VecOf<dfloat> { using S = float4; using G = float4; static constexpr int GB = 16; };
+
+// FP64 and double-float: the arithmetic is the limit (FP64 issue, or FP32
+// issue at ~12 instructions a double-float operation), so the hop pairs
+// share their reconstruction (hop_pair_sd).
+template <typename T> struct Wide : std::false_type {};
+template <> struct Wide<double> : std::true_type {};
+template <> struct Wide<dfloat> : std::true_type {};
 
 // Bytes of one gauge vector element (float2 / float4 / double2) per recon.
 template <typename T, int RECON>
@@ -345,23 +393,24 @@ __device__ __forceinline__ void hop_pair(const DslashArgs<T> &a, int h, const Nb
     reconstruct<MU, -ISIGN>(acc, w);
 }
 
-// FP64 (issue-bound on the FP64 pipe): the backward coefficients of the lower
-// spin components are the forward ones negated, so with S = w_f + w_b (the
-// backward product's FMA chains start from w_f) and D = w_f - w_b = 2 w_f - S
-// the hop pair adds S to the upper and c D to the lower components: 12 fewer
-// FP64 operations per direction than two separate reconstructions.
-template <int ND, int RECON, int ISIGN, int MU>
-__device__ __forceinline__ void hop_pair_sd(const DslashArgs<double> &a, int h, const Nbr &n, cx<double> (&acc)[4][3]) {
-    using F = Field<double>;
+// FP64 and double-float (issue-bound): the backward coefficients of the
+// lower spin components are the forward ones negated, so with S = w_f + w_b
+// (the backward product's FMA chains start from w_f) and D = w_f - w_b =
+// 2 w_f - S the hop pair adds S to the upper and c D to the lower
+// components: 12 fewer operations per direction than two separate
+// reconstructions.
+template <typename T, int ND, int RECON, int ISIGN, int MU>
+__device__ __forceinline__ void hop_pair_sd(const DslashArgs<T> &a, int h, const Nbr &n, cx<T> (&acc)[4][3]) {
+    using F = Field<T>;
     using P = Proj<MU>;
     constexpr int f = ISIGN > 0 ? 0 : 1;  // the forward hop's sign flip
     const int ps = 1 - a.pt;
-    cx<double> s[4][3], hs[2][3], w[2][3], U[3][3];
+    cx<T> s[4][3], hs[2][3], w[2][3], U[3][3];
     F::load_spinor(a.psi, a.g.stride, n.f[MU], s);
     F::template load_link<RECON, true>(a.gauge + (size_t)(a.pt * ND + MU) * a.link_block_bytes, a.g.stride, h, U);
     project<MU, ISIGN>(s, hs);
     su3_mul<false>(U, hs, w);
-    cx<double> wf[2][3];
+    cx<T> wf[2][3];
 #pragma unroll
     for (int k = 0; k < 2; k++)
 #pragma unroll
@@ -372,9 +421,9 @@ __device__ __forceinline__ void hop_pair_sd(const DslashArgs<double> &a, int h, 
     su3_mul_acc<true>(U, hs, w);  // w = S
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        cx<double> d[2];
+        cx<T> d[2];
 #pragma unroll
-        for (int k = 0; k < 2; k++) d[k] = {fma(2.0, wf[k][c].r, -w[k][c].r), fma(2.0, wf[k][c].i, -w[k][c].i)};
+        for (int k = 0; k < 2; k++) d[k] = {fma(T(2), wf[k][c].r, -w[k][c].r), fma(T(2), wf[k][c].i, -w[k][c].i)};
         acc[0][c] = cadd(acc[0][c], w[0][c]);
         acc[1][c] = cadd(acc[1][c], w[1][c]);
         acc[2][c] = cadd(acc[2][c], mulc<P::b2 ^ f>(d[P::k2]));
@@ -384,7 +433,7 @@ __device__ __forceinline__ void hop_pair_sd(const DslashArgs<double> &a, int h, 
 
 template <typename T, int ND, int RECON, int ISIGN, int MU>
 __device__ __forceinline__ void hop_pair_any(const DslashArgs<T> &a, int h, const Nbr &n, cx<T> (&acc)[4][3]) {
-    if constexpr (sizeof(T) == 8) hop_pair_sd<ND, RECON, ISIGN, MU>(a, h, n, acc);
+    if constexpr (Wide<T>::value) hop_pair_sd<T, ND, RECON, ISIGN, MU>(a, h, n, acc);
     else hop_pair<T, ND, RECON, ISIGN, MU>(a, h, n, acc);
 }
 
@@ -425,6 +474,9 @@ __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks) d
 template <typename T> struct Variants;
 template <> struct Variants<float> { static constexpr int n = 5; static constexpr int minb[5] = {0, 6, 7, 8, 10}; };
 template <> struct Variants<double> { static constexpr int n = 3; static constexpr int minb[3] = {0, 3, 4}; };
+// double-float at 32^3x64: 1.28 ms uncapped, 0.86 ms at 3 and 0.74 ms at 4
+// CTAs of 128 threads per SM; 5 and 6 spill 1.2-1.9 KB and lose
+template <> struct Variants<dfloat> { static constexpr int n = 3; static constexpr int minb[3] = {0, 3, 4}; };
 
 // Launch with the programmatic-serialisation attribute (see pdl_wait_prev).
 template <typename... P, typename... A>
@@ -491,13 +543,18 @@ __device__ __forceinline__ void block_sum_to(double *partials, T v) {
     }
 }
 
+// double-float: the per-thread sum goes in as one double
+__device__ __forceinline__ void block_sum_to(double *partials, dfloat v) {
+    block_sum_to<double>(partials, (double)v.hi + (double)v.lo);
+}
+
 template <typename T, int RECON, int ISIGN, int MINB>
 __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks)
     dslash_xpay_kernel(const DslashArgs<T> a, const typename VecOf<T>::S *__restrict__ x, T coef, double *partials) {
     pdl_allow_next();
     pdl_wait_prev();
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    T nrm = 0;
+    T nrm = T(0);
     if (h < a.g.Vh) {
         Nbr n;
         neighbours<4>(a.g, h, a.pt, n);
@@ -523,12 +580,16 @@ __global__ void __launch_bounds__(Bounds<MINB>::threads, Bounds<MINB>::blocks)
             }
         Field<T>::store_spinor(a.res, a.g.stride, h, acc);
     }
-    if (partials) block_sum_to<T>(partials, nrm);
+    if (partials) {
+        if constexpr (std::is_same_v<T, dfloat>) block_sum_to(partials, nrm);
+        else block_sum_to<T>(partials, nrm);
+    }
 }
 
 template <typename T> struct XpayMinb;
 template <> struct XpayMinb<float> { static constexpr int r18 = 6, r12 = 6; };
 template <> struct XpayMinb<double> { static constexpr int r18 = 0, r12 = 0; };
+template <> struct XpayMinb<dfloat> { static constexpr int r18 = 4, r12 = 4; };
 
 // Grid blocks of an xpay launch (the size `partials` must have).
 inline int xpay_blocks(const Geom &g) { return (g.Vh + 127) / 128; }
@@ -558,22 +619,15 @@ cudaError_t launch_dslash_xpay_t(const Geom &g, int recon, const void *gauge, co
     return cudaGetLastError();
 }
 
-// A template (not explicit specialisations), so that the variant kernels are
-// instantiated only in the translation units that launch them.
-template <typename T>
-void launch_minb(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, int minb, cudaStream_t s) {
-    if constexpr (sizeof(T) == 4) {
-        switch (minb) {
-        case 6: launch_variant<T, 6>(a, grid, block, nd, recon, isign, s); break;
-        case 7: launch_variant<T, 7>(a, grid, block, nd, recon, isign, s); break;
-        case 8: launch_variant<T, 8>(a, grid, block, nd, recon, isign, s); break;
-        default: launch_variant<T, 10>(a, grid, block, nd, recon, isign, s); break;
-        }
-    } else {
-        switch (minb) {
-        case 3: launch_variant<T, 3>(a, grid, block, nd, recon, isign, s); break;
-        default: launch_variant<T, 4>(a, grid, block, nd, recon, isign, s); break;
-        }
+// Variant I of Variants<T> (a template, so that the variant kernels are
+// instantiated only in the translation units that launch them, and only
+// those the list names).
+template <typename T, int I = 0>
+void launch_variant_index(const DslashArgs<T> &a, dim3 grid, int block, int nd, int recon, int isign, int variant,
+                          cudaStream_t s) {
+    if constexpr (I < Variants<T>::n) {
+        if (variant == I) launch_variant<T, Variants<T>::minb[I]>(a, grid, block, nd, recon, isign, s);
+        else launch_variant_index<T, I + 1>(a, grid, block, nd, recon, isign, variant, s);
     }
 }
 
@@ -592,10 +646,7 @@ cudaError_t launch_dslash_t(const Geom &g, int recon, const void *gauge, const v
     if (block <= 0) block = 128;
     if (Variants<T>::minb[variant] > 0) block = 128;  // the register cap assumes 128-thread blocks
     const dim3 grid((g.Vh + block - 1) / block);
-    switch (Variants<T>::minb[variant]) {
-    case 0: launch_variant<T, 0>(a, grid, block, g.nd, recon, isign, stream); break;
-    default: launch_minb<T>(a, grid, block, g.nd, recon, isign, Variants<T>::minb[variant], stream); break;
-    }
+    launch_variant_index<T>(a, grid, block, g.nd, recon, isign, variant, stream);
     count_launch();
     return cudaGetLastError();
 }

@@ -46,11 +46,23 @@ cudaError_t launch_dslash_xpay_f32(const Geom &g, int recon, const void *gauge, 
 cudaError_t launch_dslash_xpay_f64(const Geom &g, int recon, const void *gauge, const void *psi, const void *x,
                                    double coef, void *res, double *partials, int isign, int cb, cudaStream_t stream);
 
+// Double-float (dslash_df.cu, dfloat.cuh): FP64 fields stored as (hi, lo)
+// FP32 pairs, 16 bytes a complex as in FP64, computed on the FP32 pipes.
+int dslash_variants_df();
+cudaError_t launch_dslash_df(const Geom &g, int recon, const void *gauge, const void *psi, void *res, int isign,
+                             int cb, int block, int variant, cudaStream_t stream);
+cudaError_t launch_dslash_xpay_df(const Geom &g, int recon, const void *gauge, const void *psi, const void *x,
+                                  double coef, void *res, double *partials, int isign, int cb, cudaStream_t stream);
+// n complex elements FP64 <-> double-float; in place allowed
+cudaError_t launch_f64_to_df(const void *in, void *out, size_t n, cudaStream_t stream);
+cudaError_t launch_df_to_f64(const void *in, void *out, size_t n, cudaStream_t stream);
+
 // site0: first caller site held by the packed buffer (0 for a full lattice).
+// df (prec 64): the internal field is double-float (dfloat.cuh).
 cudaError_t launch_pack_spinor(const Geom &g, int prec, const void *psi_packed, const int *site_table,
-                               int site0, int parity, void *spinor, cudaStream_t stream);
+                               int site0, int parity, void *spinor, cudaStream_t stream, bool df = false);
 cudaError_t launch_unpack_spinor(const Geom &g, int prec, const void *spinor, const int *site_table,
-                                 int site0, int parity, void *psi_packed, cudaStream_t stream);
+                                 int site0, int parity, void *psi_packed, cudaStream_t stream, bool df = false);
 cudaError_t launch_pack_gauge(const Geom &g, int prec, int recon, const void *u_packed,
                               const int *site_table, void *gauge, cudaStream_t stream);
 

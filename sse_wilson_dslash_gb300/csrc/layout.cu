@@ -9,15 +9,43 @@
 // (lib/shift_tables_scalar.c:240-263).
 #include <cuda_runtime.h>
 
+#include <cstring>
+
+#include "dfloat.cuh"
 #include "gbds_internal.h"
 
 namespace gbds {
 
 namespace {
 
+// DF: the internal FP64 field is stored as double-float (dfloat.cuh); one
+// 16-byte unit is one complex either way
+template <bool DF>
+__device__ __forceinline__ uint4 to_internal(uint4 v) {
+    if constexpr (DF) {
+        double2 d;
+        memcpy(&d, &v, 16);
+        const float4 f = df_from_double2(d);
+        memcpy(&v, &f, 16);
+    }
+    return v;
+}
+
+template <bool DF>
+__device__ __forceinline__ uint4 to_packed(uint4 v) {
+    if constexpr (DF) {
+        float4 f;
+        memcpy(&f, &v, 16);
+        const double2 d = df_to_double2(f);
+        memcpy(&v, &d, 16);
+    }
+    return v;
+}
+
 // Spinors move as 16-byte units: FP32 = 6 units (float4), FP64 = 12 (double2).
 // `site0` is subtracted from the caller index before addressing `packed`, so
 // a buffer that holds only sites [site0, site0 + Vh) can be used.
+template <bool DF>
 __global__ void pack_spinor_kernel(const uint4 *__restrict__ packed, const int *__restrict__ table, int site0,
                                    int parity, int Vh, int stride, int units, uint4 *__restrict__ soa) {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -25,9 +53,10 @@ __global__ void pack_spinor_kernel(const uint4 *__restrict__ packed, const int *
     const int k = (int)(tid / Vh), h = (int)(tid % Vh);
     const int i = parity * Vh + h;
     const int c = table ? __ldg(table + i) : i;
-    soa[(size_t)k * stride + h] = __ldg(packed + (size_t)(c - site0) * units + k);
+    soa[(size_t)k * stride + h] = to_internal<DF>(__ldg(packed + (size_t)(c - site0) * units + k));
 }
 
+template <bool DF>
 __global__ void unpack_spinor_kernel(const uint4 *__restrict__ soa, const int *__restrict__ table, int site0,
                                      int parity, int Vh, int stride, int units, uint4 *__restrict__ packed) {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -35,7 +64,7 @@ __global__ void unpack_spinor_kernel(const uint4 *__restrict__ soa, const int *_
     const int h = (int)(tid / units), k = (int)(tid % units);
     const int i = parity * Vh + h;
     const int c = table ? __ldg(table + i) : i;
-    packed[(size_t)(c - site0) * units + k] = __ldg(soa + (size_t)k * stride + h);
+    packed[(size_t)(c - site0) * units + k] = to_packed<DF>(__ldg(soa + (size_t)k * stride + h));
 }
 
 // One thread per (parity, mu, h): reads the packed 3x3 link (transposed,
@@ -95,7 +124,7 @@ constexpr int kSpinorTile = 128;  // sites per block
 constexpr int kGaugeTile = 32;
 
 // packed: first site of checkerboard `parity` (sites [0, Vh) of that half).
-template <int UNITS>
+template <int UNITS, bool DF = false>
 __global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int Vh, int stride, uint4 *__restrict__ soa) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
     const int h0 = blockIdx.x * kSpinorTile;
@@ -105,18 +134,18 @@ __global__ void __launch_bounds__(128) pack_spinor_tile(const uint4 *packed, int
     __syncthreads();
     for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
         const int k = e / n, t = e - k * n;
-        soa[(size_t)k * stride + h0 + t] = sm[t * UNITS + k];
+        soa[(size_t)k * stride + h0 + t] = to_internal<DF>(sm[t * UNITS + k]);
     }
 }
 
-template <int UNITS>
+template <int UNITS, bool DF = false>
 __global__ void __launch_bounds__(128) unpack_spinor_tile(const uint4 *__restrict__ soa, int Vh, int stride, uint4 *packed) {
     __shared__ uint4 sm[kSpinorTile * UNITS];
     const int h0 = blockIdx.x * kSpinorTile;
     const int n = min(kSpinorTile, Vh - h0);
     for (int e = threadIdx.x; e < n * UNITS; e += blockDim.x) {
         const int k = e / n, t = e - k * n;
-        sm[t * UNITS + k] = __ldg(soa + (size_t)k * stride + h0 + t);
+        sm[t * UNITS + k] = to_packed<DF>(__ldg(soa + (size_t)k * stride + h0 + t));
     }
     __syncthreads();
     uint4 *dst = packed + (size_t)h0 * UNITS;
@@ -176,40 +205,46 @@ size_t gauge_block_bytes(const Geom &g, int prec, int recon) {
 size_t gauge_bytes(const Geom &g, int prec, int recon) { return 2 * (size_t)g.nd * gauge_block_bytes(g, prec, recon); }
 
 cudaError_t launch_pack_spinor(const Geom &g, int prec, const void *psi_packed, const int *site_table,
-                               int site0, int parity, void *spinor, cudaStream_t stream) {
+                               int site0, int parity, void *spinor, cudaStream_t stream, bool df) {
     const int units = prec == 32 ? 6 : 12;
+    df = df && prec == 64;
     if (!site_table) {
         // canonical: the checkerboard is the contiguous run [parity*Vh, parity*Vh + Vh) - site0
         const uint4 *src = static_cast<const uint4 *>(psi_packed) + (size_t)(parity * g.Vh - site0) * units;
         const unsigned nb = blocks_for(g.Vh, kSpinorTile);
-        if (prec == 32) pack_spinor_tile<6><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, static_cast<uint4 *>(spinor));
-        else pack_spinor_tile<12><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, static_cast<uint4 *>(spinor));
+        uint4 *dst = static_cast<uint4 *>(spinor);
+        if (prec == 32) pack_spinor_tile<6><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, dst);
+        else if (df) pack_spinor_tile<12, true><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, dst);
+        else pack_spinor_tile<12><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, dst);
         count_launch();
         return cudaGetLastError();
     }
     const long long n = (long long)units * g.Vh;
-    pack_spinor_kernel<<<blocks_for(n, 256), 256, 0, stream>>>(static_cast<const uint4 *>(psi_packed), site_table,
-                                                               site0, parity, g.Vh, g.stride, units,
-                                                               static_cast<uint4 *>(spinor));
+    auto k = df ? pack_spinor_kernel<true> : pack_spinor_kernel<false>;
+    k<<<blocks_for(n, 256), 256, 0, stream>>>(static_cast<const uint4 *>(psi_packed), site_table, site0, parity, g.Vh,
+                                              g.stride, units, static_cast<uint4 *>(spinor));
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_unpack_spinor(const Geom &g, int prec, const void *spinor, const int *site_table,
-                                 int site0, int parity, void *psi_packed, cudaStream_t stream) {
+                                 int site0, int parity, void *psi_packed, cudaStream_t stream, bool df) {
     const int units = prec == 32 ? 6 : 12;
+    df = df && prec == 64;
+    const uint4 *src = static_cast<const uint4 *>(spinor);
     if (!site_table) {
         uint4 *dst = static_cast<uint4 *>(psi_packed) + (size_t)(parity * g.Vh - site0) * units;
         const unsigned nb = blocks_for(g.Vh, kSpinorTile);
-        if (prec == 32) unpack_spinor_tile<6><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), g.Vh, g.stride, dst);
-        else unpack_spinor_tile<12><<<nb, 128, 0, stream>>>(static_cast<const uint4 *>(spinor), g.Vh, g.stride, dst);
+        if (prec == 32) unpack_spinor_tile<6><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, dst);
+        else if (df) unpack_spinor_tile<12, true><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, dst);
+        else unpack_spinor_tile<12><<<nb, 128, 0, stream>>>(src, g.Vh, g.stride, dst);
         count_launch();
         return cudaGetLastError();
     }
     const long long n = (long long)units * g.Vh;
-    unpack_spinor_kernel<<<blocks_for(n, 256), 256, 0, stream>>>(static_cast<const uint4 *>(spinor), site_table,
-                                                                 site0, parity, g.Vh, g.stride, units,
-                                                                 static_cast<uint4 *>(psi_packed));
+    auto k = df ? unpack_spinor_kernel<true> : unpack_spinor_kernel<false>;
+    k<<<blocks_for(n, 256), 256, 0, stream>>>(src, site_table, site0, parity, g.Vh, g.stride, units,
+                                              static_cast<uint4 *>(psi_packed));
     count_launch();
     return cudaGetLastError();
 }

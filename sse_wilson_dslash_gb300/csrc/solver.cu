@@ -115,6 +115,24 @@ __global__ void __launch_bounds__(kThreads) xmy_norm(const double2 *__restrict__
     block_sum_to<double>(partials, nrm);
 }
 
+// r = c - v for v in double-float (the outer residual's M x); partial |r|^2
+__global__ void __launch_bounds__(kThreads) xmy_norm_df(const double2 *__restrict__ c, const float4 *__restrict__ v,
+                                                       double2 *r, int Vh, int stride, double *partials) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    double nrm = 0;
+    if (h < Vh) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+            const size_t i = (size_t)k * stride + h;
+            const double2 m = df_to_double2(v[i]);
+            const double2 d = make_double2(c[i].x - m.x, c[i].y - m.y);
+            r[i] = d;
+            nrm += norm_v(d);
+        }
+    }
+    block_sum_to<double>(partials, nrm);
+}
+
 // partial |v|^2, and optionally dst = v
 template <typename T>
 __global__ void __launch_bounds__(kThreads) norm_copy(const SV<T> *__restrict__ v, SV<T> *dst, SV<T> *dst2, int Vh,
@@ -353,6 +371,9 @@ struct gbds_solver_s {
     gbds_solver_params prm;
     void *gauge64 = nullptr;  // FP64, recon 18
     void *gauge32 = nullptr;  // FP32, inner recon
+    // mixed solves: the outer residual's operator in double-float (dfloat.cuh)
+    // on the FP32 pipes: the links, and the solution converted for it
+    void *gauge_df = nullptr, *xdf = nullptr;
     // FP64 fields (checkerboard 0 except t64: checkerboard 1)
     void *b64 = nullptr, *c64 = nullptr, *x64 = nullptr, *r64 = nullptr, *p64 = nullptr, *Ap64 = nullptr,
          *Mp64 = nullptr, *t64 = nullptr;
@@ -402,6 +423,47 @@ cudaError_t apply_M(gbds_solver s, const void *gauge, int recon, const void *in,
     cudaError_t e = dslash<T>(g, recon, gauge, in, tmp, isign, 0, block, variant, st);
     if (e != cudaSuccess) return e;
     return dslash_xpay<T>(g, recon, gauge, tmp, in, (T)(-k2), out, partials, isign, 1, st);
+}
+
+// The outer residual's operator in double-float: out (double-float, in the
+// storage of an FP64 field) = M in for the FP64 field `in`, which is
+// converted into xdf first.  About 48 significant bits: the residual
+// b - M x is exact to ~1e-14 |b|, far below the tolerances the defect
+// correction reaches, at a fraction of the FP64 operator's time (GB300 issues
+// FP64 at 1/64 of the FP32 rate).
+constexpr int kDfVariant = 2;  // registers capped for 4 CTAs of 128 threads
+
+cudaError_t apply_M_df(gbds_solver s, const void *in64, void *out_df, int isign, cudaStream_t st) {
+    const Geom &g = s->g;
+    const double k2 = s->prm.kappa * s->prm.kappa;
+    cudaError_t e = launch_f64_to_df(in64, s->xdf, spinor_bytes(g, 64) / 16, st);
+    if (e == cudaSuccess) e = launch_dslash_df(g, 18, s->gauge_df, s->xdf, s->t64, isign, 0, 128, kDfVariant, st);
+    if (e != cudaSuccess) return e;
+    return launch_dslash_xpay_df(g, 18, s->gauge_df, s->t64, s->xdf, -k2, out_df, nullptr, isign, 1, st);
+}
+
+// Fields within FP32's exponent range (the double-float operator's): |b|^2
+// well inside it, else the FP64 operator forms the residual.
+bool df_range(double b2) { return b2 > 1e-50 && b2 < 1e50; }
+
+// r = b - M x (FP64 fields), partial |r|^2 in s->partials
+cudaError_t outer_residual(gbds_solver s, const void *b64, const void *x64, void *r64, bool df, cudaStream_t st) {
+    const Geom &g = s->g;
+    const int nb = blocks(g);
+    cudaError_t e;
+    if (df && s->gauge_df) {
+        e = apply_M_df(s, x64, s->Mp64, +1, st);
+        if (e != cudaSuccess) return e;
+        xmy_norm_df<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(b64), static_cast<const float4 *>(s->Mp64),
+                                             static_cast<double2 *>(r64), g.Vh, g.stride, s->partials);
+    } else {
+        e = apply_M<double>(s, s->gauge64, 18, x64, s->t64, s->Mp64, +1, nullptr, st);
+        if (e != cudaSuccess) return e;
+        xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(b64), static_cast<const double2 *>(s->Mp64),
+                                          static_cast<double2 *>(r64), g.Vh, g.stride, s->partials);
+    }
+    count_launch();
+    return cudaGetLastError();
 }
 
 // A low-precision inner solve whose residual has not dropped below 0.9 of its
@@ -530,7 +592,8 @@ cudaError_t zero(gbds_solver s, void *v, cudaStream_t st) {
 }
 
 void release(gbds_solver s) {
-    void *bufs[] = {s->gauge64, s->gauge32, s->b64, s->c64, s->x64, s->r64, s->p64, s->Ap64, s->Mp64, s->t64,
+    void *bufs[] = {s->gauge64, s->gauge32, s->gauge_df, s->xdf, s->b64, s->c64, s->x64, s->r64, s->p64, s->Ap64,
+                    s->Mp64, s->t64,
                     s->e32, s->r32, s->p32, s->Ap32, s->Mp32, s->t32, s->p16, s->Ap16, s->Mp16, s->t16, s->gauge16,
                     s->partials, s->sc};
     for (void *b : bufs)
@@ -579,6 +642,8 @@ extern "C" int gbds_solver_create(gbds_solver *out, const int dims[4], const gbd
         if (e == cudaSuccess) e = cudaMalloc(&s->gauge16, gauge_bytes(g, 32, p->inner_recon) / 2);
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->gauge64, gauge_bytes(g, 64, 18));
+    if (e == cudaSuccess && p->inner_prec != 64) e = cudaMalloc(&s->gauge_df, gauge_bytes(g, 64, 18));
+    if (e == cudaSuccess && p->inner_prec != 64) e = cudaMalloc(&s->xdf, f64);
     if (e == cudaSuccess) e = cudaMalloc(&s->partials, sizeof(double) * (size_t)blocks(g));
     if (e == cudaSuccess) e = cudaMalloc(&s->sc, sizeof(Scalars));
     if (e == cudaSuccess) e = cudaMallocHost(&s->hsc, sizeof(Scalars));
@@ -605,6 +670,7 @@ extern "C" int gbds_solver_set_gauge(gbds_solver s, const double *u_packed, void
         return set_error(GBDS_ERROR_INVALID_VALUE, "u_packed must be a 16-byte aligned device pointer");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = launch_pack_gauge(s->g, 64, 18, u_packed, nullptr, s->gauge64, st);
+    if (e == cudaSuccess && s->gauge_df) e = launch_f64_to_df(s->gauge64, s->gauge_df, gauge_bytes(s->g, 64, 18) / 16, st);
     if (e == cudaSuccess && s->prm.inner_prec != 64) {
         const size_t n = (size_t)s->g.V * 72;
         float *tmp = nullptr;
@@ -722,18 +788,13 @@ static int solve_mixed(gbds_solver s, const double *b_packed, double *x_packed, 
         total += it;
         out.cycles++;
         if (e != cudaSuccess) break;
-        // x += |c| e (the correction A^-1 M^+ r);  r = b - M x in FP64
+        // x += |c| e (the correction A^-1 M^+ r);  r = b - M x (FP64 fields,
+        // the operator in double-float)
         promote_scaled<<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->e32), std::sqrt(n2),
                                                 static_cast<double2 *>(s->x64), g.Vh, g.stride);
         count_launch();
         e = cudaGetLastError();
-        if (e == cudaSuccess) e = apply_M<double>(s, s->gauge64, 18, s->x64, s->t64, s->Mp64, +1, nullptr, st);
-        if (e == cudaSuccess) {
-            xmy_norm<<<nb, kThreads, 0, st>>>(static_cast<const double2 *>(s->b64), static_cast<const double2 *>(s->Mp64),
-                                              static_cast<double2 *>(s->r64), g.Vh, g.stride, s->partials);
-            count_launch();
-            e = cudaGetLastError();
-        }
+        if (e == cudaSuccess) e = outer_residual(s, s->b64, s->x64, s->r64, df_range(b2), st);
         if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
         if (e == cudaSuccess) e = read_scalars(s, st);
         if (e != cudaSuccess) break;
@@ -1327,7 +1388,6 @@ extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double
     const auto t0 = std::chrono::steady_clock::now();
     const Geom &g = s->g;
     const int nr = b->nrhs;
-    const int nb1 = blocks(g);
     const long long n = bcount(b);
     const size_t cs = bcs(b);
     const double tol2 = s->prm.tol * s->prm.tol;
@@ -1436,14 +1496,7 @@ extern "C" int gbds_bsolver_solve(gbds_bsolver b, const double *b_packed, double
         }
         for (int q = 0; q < nr && e == cudaSuccess; q++) {
             if (target[q] == 0.0) continue;
-            e = apply_M<double>(s, s->gauge64, 18, b->x64[q], s->t64, s->Mp64, +1, nullptr, st);
-            if (e == cudaSuccess) {
-                xmy_norm<<<nb1, kThreads, 0, st>>>(static_cast<const double2 *>(b->b64[q]),
-                                                   static_cast<const double2 *>(s->Mp64), static_cast<double2 *>(b->r64[q]),
-                                                   g.Vh, g.stride, s->partials);
-                count_launch();
-                e = cudaGetLastError();
-            }
+            e = outer_residual(s, b->b64[q], b->x64[q], b->r64[q], df_range(b2[q]), st);
             if (e == cudaSuccess) e = finish_on(s, kOuterRR, st);
             if (e == cudaSuccess) e = read_scalars(s, st);
             if (e != cudaSuccess) break;

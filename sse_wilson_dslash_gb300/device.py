@@ -33,9 +33,11 @@ class DslashOperator:
 
     dims: (Lx, Ly, Lz, Lt); nd: 4 (4D, QDP++ cb2 order) or 3 (spatial, cb3d);
     prec: 32 or 64; recon: 18 or 12 (12-real links, SU(3) only).
+    spinor_format "double_float" (prec 64, one rhs): FP64 fields held and
+    computed as hi + lo FP32 pairs on the FP32 pipes.
     """
 
-    FORMATS = {"native": 0, "bf16": 1, "f16": 2, "f32_pairs": 3}
+    FORMATS = {"native": 0, "bf16": 1, "f16": 2, "f32_pairs": 3, "double_float": 4}
 
     def __init__(self, dims, nd: int = 4, prec: int = 32, recon: int = 18, device=None, nrhs: int = 1,
                  spinor_format: str = "native"):
@@ -223,7 +225,7 @@ class DslashOperator:
         """Compulsory HBM bytes per output site and right-hand side: 2 spinors +
         2*nd links shared by the nrhs right-hand sides."""
         real = 4 if self.prec == 32 else 8
-        spinor = {"native": 24 * real, "bf16": 48, "f16": 52, "f32_pairs": 96}[self.spinor_format]
+        spinor = {"native": 24 * real, "bf16": 48, "f16": 52, "f32_pairs": 96, "double_float": 192}[self.spinor_format]
         return 2 * spinor + 2 * self.nd * self.recon * real / self.nrhs
 
 

@@ -301,3 +301,25 @@ def test_site_order_validation_and_defaults(libs):
         assert order() == want, (nrhs, fmt)
         L.gbds_op_destroy(h)
 
+
+def test_double_float_format_validation(libs):
+    """GBDS_SPINOR_DOUBLE_FLOAT (4): prec 64 and one rhs, 3D or 4D; fields of
+    the FP64 size; the FP64 register-cap variants; no site order."""
+    from sse_wilson_dslash_gb300 import _lib
+    L = _lib.core()
+    h = ctypes.c_void_p()
+    d = (ctypes.c_int * 4)(4, 4, 4, 6)
+    assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 32, 18, 1, 4) == 5
+    assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 64, 18, 2, 4) == 5
+    assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 64, 18, 1, 5) == 1
+    for nd in (4, 3):
+        assert L.gbds_op_create_ex(ctypes.byref(h), d, nd, 64, 12, 1, 4) == 0
+        ref = ctypes.c_void_p()
+        assert L.gbds_op_create_ex(ctypes.byref(ref), d, nd, 64, 12, 1, 0) == 0
+        assert L.gbds_op_spinor_bytes(h) == L.gbds_op_spinor_bytes(ref)
+        assert L.gbds_op_gauge_bytes(h) == L.gbds_op_gauge_bytes(ref)
+        assert L.gbds_op_num_variants(h) == L.gbds_op_num_variants(ref) == 3
+        assert L.gbds_op_set_site_order(h, 2) == 5
+        L.gbds_op_destroy(ref)
+        L.gbds_op_destroy(h)
+
