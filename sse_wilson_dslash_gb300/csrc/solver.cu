@@ -431,7 +431,7 @@ cudaError_t apply_M(gbds_solver s, const void *gauge, int recon, const void *in,
 // b - M x is exact to ~1e-14 |b|, far below the tolerances the defect
 // correction reaches, at a fraction of the FP64 operator's time (GB300 issues
 // FP64 at 1/64 of the FP32 rate).
-constexpr int kDfVariant = 2;  // registers capped for 4 CTAs of 128 threads
+constexpr int kDfVariant = 0;  // the colour-split kernel (dslash_df.cu)
 
 cudaError_t apply_M_df(gbds_solver s, const void *in64, void *out_df, int isign, cudaStream_t st) {
     const Geom &g = s->g;

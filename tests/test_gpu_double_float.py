@@ -45,6 +45,31 @@ def test_double_float_matches_oracle(nd, dims, layout_kind, recon):
     op.close()
 
 
+@pytest.mark.parametrize("nd,dims", [(4, (8, 4, 6, 4)), (3, (4, 6, 4, 5)), (4, (2, 2, 2, 2)), (4, (6, 2, 2, 10))])
+def test_double_float_variants_match_oracle(nd, dims):
+    """Every variant: 0 the colour-split kernel (three warps a CTA, 32 sites;
+    (6, 2, 2, 10) and (2, 2, 2, 2) leave the last CTA partly idle), 1-2 the
+    one-thread-per-site kernel with register caps."""
+    import torch
+    from sse_wilson_dslash_gb300.device import DslashOperator
+    lol = O.layout_table(O.LAYOUT_CB2 if nd == 4 else O.LAYOUT_CB3D, dims)
+    u, psi = O.make_inputs(dims, 33, 34)
+    for variant in range(3):
+        op = DslashOperator(dims, nd=nd, prec=64, recon=18, spinor_format="double_float")
+        op.set_tuning(0, variant)
+        V = op.volume
+        gauge = op.pack_gauge(torch.from_numpy(np.ascontiguousarray(u)).cuda())
+        pd = torch.from_numpy(np.ascontiguousarray(psi)).cuda()
+        for isign, cb in ((1, 1), (-1, 0)):
+            out = op.apply(gauge, op.pack_spinor(pd, cb), isign, cb)
+            res = torch.zeros(V * 24, dtype=torch.float64, device="cuda")
+            op.unpack_spinor(out, 1 - cb, res)
+            ref = O.dslash_plain(nd, dims, lol, u, psi, isign, cb)
+            err = O.site_rel_err(res.cpu().numpy(), ref, O.target_sites(nd, dims, lol, cb))
+            assert err <= DF_TOL, (variant, isign, cb, err)
+        op.close()
+
+
 def test_double_float_pack_round_trip():
     """pack -> unpack keeps 48 significant bits of every double (relative
     error <= 2^-47) and FP32-representable values exactly."""
