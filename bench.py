@@ -17,9 +17,10 @@ line on rank 0:
               over its CUDA-event time, against MEASURED_PEAKS.json
   cpu_baseline the oracle's table-driven port (OpenMP) on the host cores, on a
               bounded slice of the same workload
-  variants    recon-12, FP64, the 3D operator on 24^3x48, several right-hand
-              sides on 24^3x48, the uneven batch, the force, one rank's slab
-              of the lattice split along t (not the headline)
+  variants    recon-12, FP64 (native and in double-float arithmetic), the 3D
+              operator on 24^3x48, several right-hand sides on 24^3x48, the
+              uneven batch, the force, one rank's slab of the lattice split
+              along t (not the headline)
 
 --impl reference times the CPU implementation of the path on the host cores:
 the reference library built from its own sources (oracle/_ref) where it was
@@ -281,9 +282,9 @@ def time_device(op, gauge, srcs, outs, steps, warmup, torch):
     return e0.elapsed_time(e1) / steps
 
 
-def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None):
+def device_variant(dims, nd, prec, recon, steps, warmup, torch, fields=None, fmt="native"):
     from sse_wilson_dslash_gb300.device import DslashOperator
-    op = DslashOperator(dims, nd=nd, prec=prec, recon=recon)
+    op = DslashOperator(dims, nd=nd, prec=prec, recon=recon, spinor_format=fmt)
     dt = torch.float32 if prec == 32 else torch.float64
     u, psi = fields if fields is not None else make_fields(dims, dt, torch)
     gauge = op.pack_gauge(u)
@@ -783,6 +784,10 @@ def run_gb300(args):
             torch.cuda.empty_cache()
             variants["f64_recon18"] = device_variant(DIMS, 4, 64, 18, vsteps, 5, torch, fields=(u64, psi64))
             variants["f64_recon12"] = device_variant(DIMS, 4, 64, 12, vsteps, 5, torch, fields=(u64, psi64))
+            # the FP64 operator in double-float arithmetic on the FP32 pipes
+            # (FP64-sized fields, ~48 significant bits)
+            variants["f64_double_float_recon18"] = device_variant(DIMS, 4, 64, 18, vsteps, 5, torch,
+                                                                  fields=(u64, psi64), fmt="double_float")
             del u64, psi64
         else:
             del u, psi

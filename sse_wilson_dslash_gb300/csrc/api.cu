@@ -74,7 +74,7 @@ int gen_zblock(const Geom &g, int nrhs, int fmt, int recon) {
     const double plane = site * g.Lxh * g.L[1];
     if (2.0 * g.L[2] * plane <= kGenReuseBytes) return 0;
     int best = 1;
-    for (int b = 2; b < g.L[2]; b++)
+    for (int b = 2; b < g.L[2] && b < 32768; b++)  // Geom holds it in 16 bits
         if (g.L[2] % b == 0 && 2.0 * b * plane <= kGenReuseBytes) best = b;
     return best;
 }
@@ -294,6 +294,7 @@ extern "C" int gbds_op_set_site_order(gbds_op op, int zblock) {
     if (zblock < 0 || zblock > Lz || (zblock > 0 && Lz % zblock != 0))
         return set_error(GBDS_ERROR_INVALID_VALUE, "zblock must be -1, 0 or a divisor of the z extent");
     if (zblock == Lz) zblock = 0;  // one slab: the natural order
+    if (zblock > 32767) return set_error(GBDS_ERROR_UNSUPPORTED, "z slabs of more than 32767 planes");
     if (zblock != 0 && !generic(op))
         return set_error(GBDS_ERROR_UNSUPPORTED, "the site order applies to operators with several right-hand sides "
                                                  "or 16-bit storage");

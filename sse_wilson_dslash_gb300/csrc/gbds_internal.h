@@ -12,16 +12,20 @@
 namespace gbds {
 
 // Lattice geometry as the kernels see it.
+// 36 bytes: the uneven-batch kernel reads an array of descriptors holding a
+// Geom from its parameters by a run-time index, and a larger stride cost it
+// register spills and 50 % of its speed.
 struct Geom {
-    int L[4];     // Lx, Ly, Lz, Lt
-    int nd;       // 4 or 3
-    int Lxh;      // Lx / 2
-    int V;        // full volume
-    int Vh;       // sites per checkerboard
-    int stride;   // elements between consecutive components of a field
-    int zblock;   // site order of the multi-RHS kernels: z slabs of this many
-                  // planes, t swept inside each (0: natural order; gen_site)
+    int L[4];      // Lx, Ly, Lz, Lt
+    short nd;      // 4 or 3
+    short zblock;  // site order of the multi-RHS kernels: z slabs of this
+                   // many planes, t swept inside each (0: natural; gen_site)
+    int Lxh;       // Lx / 2
+    int V;         // full volume
+    int Vh;        // sites per checkerboard
+    int stride;    // elements between consecutive components of a field
 };
+static_assert(sizeof(Geom) == 36, "Geom is part of the uneven batch's parameter block");
 
 // Record an error message for gbds_get_last_error() and return `code`.
 int set_error(int code, const std::string &msg);
