@@ -129,6 +129,48 @@ def test_batched_solve_matches_single_solves(nrhs, inner_recon):
     bsolver.close()
 
 
+@pytest.mark.parametrize("scale", [1e30, 1e-30, 1.0])
+def test_outer_residual_outside_the_double_float_range(scale):
+    """The outer residual b - M x runs in double-float (FP32 exponent range)
+    when |b|^2 lies in [1e-50, 1e50] and on the FP64 operator otherwise:
+    sources scaled by 1e30 and 1e-30 take the FP64 path, 1.0 the double-float
+    one, and all three reach 1e-10 with the oracle's |b - M x| / |b| below
+    1e-8; in the batched solver each rhs takes its own path (one scaled, one
+    not)."""
+    import torch
+    from sse_wilson_dslash_gb300.device import BatchedWilsonSolver, WilsonSolver
+    dims = (8, 8, 4, 8)
+    V = O.volume(dims)
+    lol = O.layout_table(O.LAYOUT_CB2, dims)
+    u, b = O.make_inputs(dims, 71, 72, kind="near_unit")
+    b = b.ravel() * scale
+    ev = O.target_sites(4, dims, lol, 1)
+
+    def true_res(xv, bv):
+        Mx, _ = _even_M(dims, lol, u, xv, KAPPA, 1)
+        return np.linalg.norm((Mx - bv.reshape(Mx.shape)).reshape(-1, 24)[ev]) / np.linalg.norm(bv.reshape(-1, 24)[ev])
+
+    ug = torch.from_numpy(u.ravel()).cuda()
+    s = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=32)
+    s.set_gauge(ug)
+    x = torch.zeros(b.size, dtype=torch.float64, device="cuda")
+    st = s.solve(torch.from_numpy(b).cuda(), x)
+    assert st["converged"] == 1 and st["residual"] <= 1e-10, st
+    assert true_res(x.cpu().numpy(), b) < 1e-8
+    s.close()
+    rng = np.random.default_rng(73)
+    b2 = np.stack([b, O.gaussian_spinor(rng, V).ravel()])
+    bsolver = BatchedWilsonSolver(dims, 2, KAPPA, tol=1e-10)
+    bsolver.set_gauge(ug)
+    xt = torch.zeros(b2.size, dtype=torch.float64, device="cuda")
+    stats = bsolver.solve(torch.from_numpy(b2.ravel()).cuda(), xt)
+    xb = xt.cpu().numpy().reshape(2, -1)
+    for q in range(2):
+        assert stats[q]["converged"] == 1, (q, stats[q])
+        assert true_res(xb[q], b2[q]) < 1e-8, q
+    bsolver.close()
+
+
 def test_batched_solver_rejects_bad_arguments():
     from sse_wilson_dslash_gb300 import _lib
     from sse_wilson_dslash_gb300.device import BatchedWilsonSolver
