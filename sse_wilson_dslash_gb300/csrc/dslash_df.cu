@@ -31,25 +31,45 @@ __global__ void df_to_f64_kernel(const float4 *in, double2 *out, size_t n) {
 // ---------------------------------------------------------------------------
 
 constexpr int kDf3Sites = 32;
-constexpr int kDf3Minb = 7;  // CTAs of 96 threads per SM the registers are capped for
+constexpr int kDf3Minb = 8;  // CTAs of 96 threads per SM the registers are capped for (80, no spills)
 
 __device__ __forceinline__ cx<dfloat> df_cx(float4 q) { return {dfloat(q.x, q.y), dfloat(q.z, q.w)}; }
 __device__ __forceinline__ float4 df_f4(const cx<dfloat> &v) { return make_float4(v.r.hi, v.r.lo, v.i.hi, v.i.lo); }
 
-// m * v (CONJ: conj(m) * v), added to acc
+// A sum of double-float products kept unnormalised: value = s + e, the
+// products' high parts summed exactly by TwoSum into s and every rounding
+// error (the products' low parts, the TwoSum errors) added into e.  12 FP32
+// instructions a product against 15 for a double-float multiply-add, one
+// TwoSum at the end; the error stays of order 2^-48 of the summed
+// magnitudes, as in the double-float operations.
+struct dsum {
+    float s, e;
+};
+
+__device__ __forceinline__ dsum dsum_of(dfloat a) { return {a.hi, a.lo}; }
+
+__device__ __forceinline__ void dsum_add_prod(dsum &a, dfloat x, dfloat y) {
+    const float p = __fmul_rn(x.hi, y.hi);
+    const float pe = df_prod_err(x, y, p);
+    const dfloat t = df_two_sum(a.s, p);
+    a.s = t.hi;
+    a.e = __fadd_rn(a.e, __fadd_rn(t.lo, pe));
+}
+
+__device__ __forceinline__ dfloat dsum_value(dsum a) { return df_two_sum(a.s, a.e); }
+
+// acc += m * v (CONJ: conj(m) * v) for the three colours j of a row
 template <bool CONJ>
-__device__ __forceinline__ void cmac(const cx<dfloat> &m, const cx<dfloat> &v, cx<dfloat> &acc) {
-    if (CONJ) {
-        acc.r = fma(m.r, v.r, acc.r);
-        acc.r = fma(m.i, v.i, acc.r);
-        acc.i = fma(m.r, v.i, acc.i);
-        acc.i = fma(-m.i, v.r, acc.i);
-    } else {
-        acc.r = fma(m.r, v.r, acc.r);
-        acc.r = fma(-m.i, v.i, acc.r);
-        acc.i = fma(m.r, v.i, acc.i);
-        acc.i = fma(m.i, v.r, acc.i);
+__device__ __forceinline__ void row_mac(const cx<dfloat> (&m)[3], const cx<dfloat> (&v)[3], cx<dfloat> &acc) {
+    dsum re = dsum_of(acc.r), im = dsum_of(acc.i);
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        dsum_add_prod(re, m[j].r, v[j].r);
+        dsum_add_prod(re, CONJ ? m[j].i : -m[j].i, CONJ ? v[j].i : v[j].i);
+        dsum_add_prod(im, m[j].r, v[j].i);
+        dsum_add_prod(im, CONJ ? -m[j].i : m[j].i, v[j].r);
     }
+    acc = {dsum_value(re), dsum_value(im)};
 }
 
 // Colour c of the projected half spinor of psi(site), exchanged: hs[k][j]
@@ -97,8 +117,7 @@ __device__ __forceinline__ void df3_dir(const DslashArgs<dfloat> &a, int h, int 
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             wf[k] = {dfloat(), dfloat()};
-#pragma unroll
-            for (int j = 0; j < 3; j++) cmac<false>(m[j], hs[k][j], wf[k]);
+            row_mac<false>(m, hs[k], wf[k]);
         }
     }
     df3_project<MU, -ISIGN>(a.psi, stride, act ? n.b[MU] : 0, c, lane, act, sm[buf], hs);
@@ -113,12 +132,13 @@ __device__ __forceinline__ void df3_dir(const DslashArgs<dfloat> &a, int h, int 
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             w[k] = wf[k];
-#pragma unroll
-            for (int j = 0; j < 3; j++) cmac<true>(m[j], hs[k][j], w[k]);  // (U^+)_cj = conj(U_jc)
+            row_mac<true>(m, hs[k], w[k]);  // (U^+)_cj = conj(U_jc)
         }
+        // D = 2 w_f - S: the doubling is exact
         cx<dfloat> d[2];
 #pragma unroll
-        for (int k = 0; k < 2; k++) d[k] = {fma(dfloat(2.f), wf[k].r, -w[k].r), fma(dfloat(2.f), wf[k].i, -w[k].i)};
+        for (int k = 0; k < 2; k++)
+            d[k] = {dfloat(2.f * wf[k].r.hi, 2.f * wf[k].r.lo) - w[k].r, dfloat(2.f * wf[k].i.hi, 2.f * wf[k].i.lo) - w[k].i};
         acc[0] = cadd(acc[0], w[0]);
         acc[1] = cadd(acc[1], w[1]);
         acc[2] = cadd(acc[2], mulc<P::b2 ^ f>(d[P::k2]));
