@@ -200,9 +200,15 @@ def run_solver_bench(torch, log_fn):
     out = {"lattice": list(dims), "kappa": 0.124, "links": "exp(i 0.3 H), H traceless Hermitian N(0,1)",
            "source": "N(0,1)", "tol": 1e-10, "residual": "|M^+ b - M^+ M x| / |M^+ b| (CG on M^+ M)"}
     sols = {}
-    for name, prec, recon, itol in (("fp64_cg", 64, 18, 1e-5), ("mixed_fp32_fp64", 32, 12, 1e-5),
-                                    ("mixed_fp16_fp64", 16, 12, 1e-3), ("mixed_bf16_fp64", 17, 12, 1e-3)):
-        s = WilsonSolver(dims, 0.124, tol=1e-10, max_iter=20000, inner_prec=prec, inner_recon=recon, inner_tol=itol)
+    # *_fp64: the outer residual on the FP64 operator (the default);
+    # *_df_outer: on the operator in double-float arithmetic (FP32 pipes)
+    for name, prec, recon, itol, dfo in (("fp64_cg", 64, 18, 1e-5, False), ("mixed_fp32_fp64", 32, 12, 1e-5, False),
+                                         ("mixed_fp16_fp64", 16, 12, 1e-3, False),
+                                         ("mixed_bf16_fp64", 17, 12, 1e-3, False),
+                                         ("mixed_fp32_df_outer", 32, 12, 1e-5, True),
+                                         ("mixed_fp16_df_outer", 16, 12, 1e-3, True)):
+        s = WilsonSolver(dims, 0.124, tol=1e-10, max_iter=20000, inner_prec=prec, inner_recon=recon, inner_tol=itol,
+                         outer_double_float=dfo)
         s.set_gauge(u)
         x = torch.zeros_like(b)
         torch.cuda.synchronize()
@@ -218,7 +224,7 @@ def run_solver_bench(torch, log_fn):
         del s
         torch.cuda.empty_cache()
     out["speedup"] = out["fp64_cg"]["wall_seconds"] / out["mixed_fp32_fp64"]["wall_seconds"]
-    for k in ("mixed_fp32_fp64", "mixed_fp16_fp64", "mixed_bf16_fp64"):
+    for k in ("mixed_fp32_fp64", "mixed_fp16_fp64", "mixed_bf16_fp64", "mixed_fp32_df_outer", "mixed_fp16_df_outer"):
         out[k]["speedup_vs_fp64"] = out["fp64_cg"]["wall_seconds"] / out[k]["wall_seconds"]
         out[k]["solution_rel_diff"] = float((sols["fp64_cg"] - sols[k]).norm() / sols["fp64_cg"].norm())
     # batched: 16 right-hand sides (the first is the source above), FP32
@@ -229,25 +235,29 @@ def run_solver_bench(torch, log_fn):
     bb[0] = b
     del sols
     torch.cuda.empty_cache()
-    bs = BatchedWilsonSolver(dims, nrhs, 0.124, tol=1e-10, max_iter=20000, inner_recon=12)
-    bs.set_gauge(u)
-    xx = torch.zeros_like(bb)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sts = bs.solve(bb, xx)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    per_rhs = wall / nrhs
-    out["batched_fp32_fp64_nrhs16"] = {
-        "nrhs": nrhs, "wall_seconds": wall, "seconds_per_rhs": per_rhs,
-        "iterations_max": max(t["iterations"] for t in sts), "cycles_max": max(t["cycles"] for t in sts),
-        "converged": int(all(t["converged"] for t in sts)), "residual_max": max(t["residual"] for t in sts),
-        "true_residual_max": max(t["true_residual"] for t in sts),
-        "speedup_per_rhs_vs_fp64": out["fp64_cg"]["wall_seconds"] / per_rhs,
-        "speedup_per_rhs_vs_mixed_fp32": out["mixed_fp32_fp64"]["wall_seconds"] / per_rhs}
-    log_fn("batched_fp32_fp64_nrhs16", out["batched_fp32_fp64_nrhs16"])
-    bs.close()
-    del bs, bb, xx
+    for name, dfo, single in (("batched_fp32_fp64_nrhs16", False, "mixed_fp32_fp64"),
+                              ("batched_fp32_df_outer_nrhs16", True, "mixed_fp32_df_outer")):
+        bs = BatchedWilsonSolver(dims, nrhs, 0.124, tol=1e-10, max_iter=20000, inner_recon=12, outer_double_float=dfo)
+        bs.set_gauge(u)
+        xx = torch.zeros_like(bb)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sts = bs.solve(bb, xx)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        per_rhs = wall / nrhs
+        out[name] = {
+            "nrhs": nrhs, "wall_seconds": wall, "seconds_per_rhs": per_rhs,
+            "iterations_max": max(t["iterations"] for t in sts), "cycles_max": max(t["cycles"] for t in sts),
+            "converged": int(all(t["converged"] for t in sts)), "residual_max": max(t["residual"] for t in sts),
+            "true_residual_max": max(t["true_residual"] for t in sts),
+            "speedup_per_rhs_vs_fp64": out["fp64_cg"]["wall_seconds"] / per_rhs,
+            f"speedup_per_rhs_vs_{single}": out[single]["wall_seconds"] / per_rhs}
+        log_fn(name, out[name])
+        bs.close()
+        del bs, xx
+        torch.cuda.empty_cache()
+    del bb
     torch.cuda.empty_cache()
     return out
 

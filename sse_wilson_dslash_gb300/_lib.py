@@ -23,7 +23,8 @@ NODENUM = ctypes.CFUNCTYPE(ctypes.c_int, c_int_p)
 class SolverParams(ctypes.Structure):
     """gbds_solver_params (include/gbdslash.h)."""
     _fields_ = [("kappa", ctypes.c_double), ("tol", ctypes.c_double), ("max_iter", ctypes.c_int),
-                ("inner_prec", ctypes.c_int), ("inner_recon", ctypes.c_int), ("inner_tol", ctypes.c_double)]
+                ("inner_prec", ctypes.c_int), ("inner_recon", ctypes.c_int), ("inner_tol", ctypes.c_double),
+                ("outer_double_float", ctypes.c_int)]
 
 
 class SolverStats(ctypes.Structure):

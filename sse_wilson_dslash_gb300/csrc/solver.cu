@@ -371,8 +371,9 @@ struct gbds_solver_s {
     gbds_solver_params prm;
     void *gauge64 = nullptr;  // FP64, recon 18
     void *gauge32 = nullptr;  // FP32, inner recon
-    // mixed solves: the outer residual's operator in double-float (dfloat.cuh)
-    // on the FP32 pipes: the links, and the solution converted for it
+    // mixed solves with outer_double_float: the outer residual's operator in
+    // double-float (dfloat.cuh) on the FP32 pipes: the links, and the
+    // solution converted for it
     void *gauge_df = nullptr, *xdf = nullptr;
     // FP64 fields (checkerboard 0 except t64: checkerboard 1)
     void *b64 = nullptr, *c64 = nullptr, *x64 = nullptr, *r64 = nullptr, *p64 = nullptr, *Ap64 = nullptr,
@@ -425,12 +426,13 @@ cudaError_t apply_M(gbds_solver s, const void *gauge, int recon, const void *in,
     return dslash_xpay<T>(g, recon, gauge, tmp, in, (T)(-k2), out, partials, isign, 1, st);
 }
 
-// The outer residual's operator in double-float: out (double-float, in the
-// storage of an FP64 field) = M in for the FP64 field `in`, which is
-// converted into xdf first.  About 48 significant bits: the residual
-// b - M x is exact to ~1e-14 |b|, far below the tolerances the defect
-// correction reaches, at a fraction of the FP64 operator's time (GB300 issues
-// FP64 at 1/64 of the FP32 rate).
+// The outer residual's operator in double-float (outer_double_float): out
+// (double-float, in the storage of an FP64 field) = M in for the FP64 field
+// `in`, which is converted into xdf first.  About 48 significant bits: the
+// residual b - M x is exact to ~1e-14 |b|, far below the tolerances the
+// defect correction reaches, at a fraction of the FP64 operator's time (GB300
+// issues FP64 at 1/64 of the FP32 rate).  By default the FP64 operator forms
+// the residual.
 constexpr int kDfVariant = 0;  // the colour-split kernel (dslash_df.cu)
 
 cudaError_t apply_M_df(gbds_solver s, const void *in64, void *out_df, int isign, cudaStream_t st) {
@@ -642,8 +644,9 @@ extern "C" int gbds_solver_create(gbds_solver *out, const int dims[4], const gbd
         if (e == cudaSuccess) e = cudaMalloc(&s->gauge16, gauge_bytes(g, 32, p->inner_recon) / 2);
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->gauge64, gauge_bytes(g, 64, 18));
-    if (e == cudaSuccess && p->inner_prec != 64) e = cudaMalloc(&s->gauge_df, gauge_bytes(g, 64, 18));
-    if (e == cudaSuccess && p->inner_prec != 64) e = cudaMalloc(&s->xdf, f64);
+    const bool df = p->inner_prec != 64 && p->outer_double_float;
+    if (e == cudaSuccess && df) e = cudaMalloc(&s->gauge_df, gauge_bytes(g, 64, 18));
+    if (e == cudaSuccess && df) e = cudaMalloc(&s->xdf, f64);
     if (e == cudaSuccess) e = cudaMalloc(&s->partials, sizeof(double) * (size_t)blocks(g));
     if (e == cudaSuccess) e = cudaMalloc(&s->sc, sizeof(Scalars));
     if (e == cudaSuccess) e = cudaMallocHost(&s->hsc, sizeof(Scalars));
@@ -718,7 +721,8 @@ extern "C" int gbds_solver_solve_normal(gbds_solver s, const double *c_packed, d
 
 // Mixed-precision solve of M x = b by defect correction on the true
 // residual: each cycle forms r = b - M x in FP64 (two FP64 Dslash
-// applications), then c = M^+ r in FP32 (the normal-equation right-hand side
+// applications, or the double-float operator with outer_double_float), then
+// c = M^+ r in FP32 (the normal-equation right-hand side
 // for the inner CG and, through |c|, the stopping test |M^+ (b - M x)| <=
 // tol |M^+ b|: the cancellation is in the FP64 subtraction, so |c| carries
 // FP32 relative accuracy of its own size), then the inner CG on M^+ M and

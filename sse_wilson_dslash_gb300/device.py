@@ -236,13 +236,15 @@ class WilsonSolver:
     packed layout ``[V][4][3][2]``, QDP++ cb2 order.
 
     inner_prec 64: all-FP64 CG.  inner_prec 32: FP32 CG inside FP64 defect
-    correction (residual, solution update and global norms in FP64)."""
+    correction (residual, solution update and global norms in FP64).
+    outer_double_float: the outer residual's operator in double-float
+    arithmetic on the FP32 pipes instead of FP64."""
 
     def __init__(self, dims, kappa: float, tol: float = 1e-10, max_iter: int = 10000, inner_prec: int = 32,
-                 inner_recon: int = 12, inner_tol: float = 1e-5):
+                 inner_recon: int = 12, inner_tol: float = 1e-5, outer_double_float: bool = False):
         self.dims = tuple(int(v) for v in dims)
         self.volume = int(np.prod(self.dims))
-        p = _lib.SolverParams(kappa, tol, max_iter, inner_prec, inner_recon, inner_tol)
+        p = _lib.SolverParams(kappa, tol, max_iter, inner_prec, inner_recon, inner_tol, int(outer_double_float))
         h = ctypes.c_void_p()
         _lib.check(_lib.core().gbds_solver_create(ctypes.byref(h), (ctypes.c_int * 4)(*self.dims), ctypes.byref(p)))
         self._h = h
@@ -289,14 +291,15 @@ class BatchedWilsonSolver:
     """``nrhs`` (2, 4, 8, 16 or 32) independent solves M x_q = b_q on one gauge
     field (gbds_bsolver_* in include/gbdslash.h): the FP32 inner CGs advance
     together on the multi-RHS operator, the FP64 defect correction runs per
-    right-hand side.  b, x: FP64 CUDA tensors ``[nrhs][V][4][3][2]``."""
+    right-hand side (outer_double_float: its operator in double-float).
+    b, x: FP64 CUDA tensors ``[nrhs][V][4][3][2]``."""
 
     def __init__(self, dims, nrhs: int, kappa: float, tol: float = 1e-10, max_iter: int = 10000,
-                 inner_recon: int = 12, inner_tol: float = 1e-5):
+                 inner_recon: int = 12, inner_tol: float = 1e-5, outer_double_float: bool = False):
         self.dims = tuple(int(v) for v in dims)
         self.volume = int(np.prod(self.dims))
         self.nrhs = int(nrhs)
-        p = _lib.SolverParams(kappa, tol, max_iter, 32, inner_recon, inner_tol)
+        p = _lib.SolverParams(kappa, tol, max_iter, 32, inner_recon, inner_tol, int(outer_double_float))
         h = ctypes.c_void_p()
         _lib.check(_lib.core().gbds_bsolver_create(ctypes.byref(h), (ctypes.c_int * 4)(*self.dims), self.nrhs,
                                                    ctypes.byref(p)))

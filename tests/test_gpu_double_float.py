@@ -107,7 +107,13 @@ def test_double_float_agrees_with_fp64_on_24x24x24x48():
     for fmt in ("native", "double_float"):
         op = DslashOperator(dims, nd=4, prec=64, spinor_format=fmt)
         gauge = op.pack_gauge(u)
-        out = op.apply(gauge, op.pack_spinor(psi, 0), -1, 0)
+        src = op.pack_spinor(psi, 0)
+        if fmt == "double_float":
+            # the autotuner picks among the colour-split kernel and the
+            # capped one-thread-per-site variants; any pick keeps the result
+            threads, variant = op.autotune(gauge, src, op.new_spinor())
+            assert 0 <= variant < op.num_variants
+        out = op.apply(gauge, src, -1, 0)
         res = torch.zeros(V * 24, dtype=torch.float64, device="cuda")
         op.unpack_spinor(out, 1, res)
         outs[fmt] = res.view(V, 24)
@@ -130,4 +136,7 @@ def test_double_float_rejects_what_it_does_not_cover():
     f = torch.empty(1 << 20, dtype=torch.uint8, device="cuda")
     with pytest.raises(_lib.GbdsError):
         op.pack_faces(op.new_gauge(), op.new_spinor(), 1, 0, f, f)
+    with pytest.raises(_lib.GbdsError):
+        op.force(op.new_gauge(), op.new_spinor(), op.new_spinor(), 1, 0,
+                 torch.empty(op.volume * 72, dtype=torch.float64, device="cuda"))
     op.close()

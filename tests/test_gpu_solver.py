@@ -39,15 +39,19 @@ def test_apply_M_matches_oracle(dagger):
     s.close()
 
 
-@pytest.mark.parametrize("inner_prec,inner_recon", [(64, 18), (32, 18), (32, 12), (16, 12), (17, 12), (16, 18)])
-def test_solve_reaches_tolerance(inner_prec, inner_recon):
+@pytest.mark.parametrize("inner_prec,inner_recon,outer_df", [(64, 18, False), (32, 18, False), (32, 12, False),
+                                                              (32, 12, True), (16, 12, False), (16, 12, True),
+                                                              (17, 12, False), (16, 18, False)])
+def test_solve_reaches_tolerance(inner_prec, inner_recon, outer_df):
+    """outer_df: the outer residual's operator in double-float instead of
+    FP64; the oracle's FP64 residual checks both."""
     import torch
     from sse_wilson_dslash_gb300.device import WilsonSolver
     dims = (8, 8, 8, 8)
     lol = O.layout_table(O.LAYOUT_CB2, dims)
     u, b = O.make_inputs(dims, 51, 52, kind="near_unit")
     s = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=inner_prec, inner_recon=inner_recon,
-                     inner_tol=1e-5 if inner_prec >= 32 else 1e-3)
+                     inner_tol=1e-5 if inner_prec >= 32 else 1e-3, outer_double_float=outer_df)
     s.set_gauge(torch.from_numpy(u.ravel()).cuda())
     x = torch.zeros(b.size, dtype=torch.float64, device="cuda")
     st = s.solve(torch.from_numpy(b.ravel()).cuda(), x)
@@ -84,8 +88,9 @@ def test_mixed_and_fp64_solutions_agree():
         assert (xs[0] - x).norm() / xs[0].norm() < 1e-9
 
 
-@pytest.mark.parametrize("nrhs,inner_recon", [(4, 12), (8, 18), (16, 12), (32, 18)])
-def test_batched_solve_matches_single_solves(nrhs, inner_recon):
+@pytest.mark.parametrize("nrhs,inner_recon,outer_df", [(4, 12, False), (8, 18, False), (16, 12, False),
+                                                        (16, 12, True), (32, 18, False)])
+def test_batched_solve_matches_single_solves(nrhs, inner_recon, outer_df):
     """The batched solver: every right-hand side reaches 1e-10, its solution
     agrees with the single-rhs mixed solve of the same system, and the
     oracle confirms |b - M x| / |b|.  One right-hand side is zero (its
@@ -102,14 +107,14 @@ def test_batched_solve_matches_single_solves(nrhs, inner_recon):
     bs = [O.gaussian_spinor(rng, V).ravel() for _ in range(nrhs)]
     bs[1] = np.zeros_like(bs[1])
     bs[3] = -2.5 * bs[2]
-    bsolver = BatchedWilsonSolver(dims, nrhs, KAPPA, tol=1e-10, inner_recon=inner_recon)
+    bsolver = BatchedWilsonSolver(dims, nrhs, KAPPA, tol=1e-10, inner_recon=inner_recon, outer_double_float=outer_df)
     ug = torch.from_numpy(u.ravel()).cuda()
     bsolver.set_gauge(ug)
     bt = torch.from_numpy(np.stack(bs).ravel()).cuda()
     xt = torch.zeros_like(bt)
     stats = bsolver.solve(bt, xt)
     x = xt.cpu().numpy().reshape(nrhs, V * 24)
-    single = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=32, inner_recon=inner_recon)
+    single = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=32, inner_recon=inner_recon, outer_double_float=outer_df)
     single.set_gauge(ug)
     ev = O.target_sites(4, dims, lol, 1)
     for q in range(nrhs):
@@ -131,8 +136,9 @@ def test_batched_solve_matches_single_solves(nrhs, inner_recon):
 
 @pytest.mark.parametrize("scale", [1e30, 1e-30, 1.0])
 def test_outer_residual_outside_the_double_float_range(scale):
-    """The outer residual b - M x runs in double-float (FP32 exponent range)
-    when |b|^2 lies in [1e-50, 1e50] and on the FP64 operator otherwise:
+    """With outer_double_float the outer residual b - M x runs in
+    double-float (FP32 exponent range) when |b|^2 lies in [1e-50, 1e50] and
+    on the FP64 operator otherwise:
     sources scaled by 1e30 and 1e-30 take the FP64 path, 1.0 the double-float
     one, and all three reach 1e-10 with the oracle's |b - M x| / |b| below
     1e-8; in the batched solver each rhs takes its own path (one scaled, one
@@ -151,7 +157,7 @@ def test_outer_residual_outside_the_double_float_range(scale):
         return np.linalg.norm((Mx - bv.reshape(Mx.shape)).reshape(-1, 24)[ev]) / np.linalg.norm(bv.reshape(-1, 24)[ev])
 
     ug = torch.from_numpy(u.ravel()).cuda()
-    s = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=32)
+    s = WilsonSolver(dims, KAPPA, tol=1e-10, inner_prec=32, outer_double_float=True)
     s.set_gauge(ug)
     x = torch.zeros(b.size, dtype=torch.float64, device="cuda")
     st = s.solve(torch.from_numpy(b).cuda(), x)
@@ -160,7 +166,7 @@ def test_outer_residual_outside_the_double_float_range(scale):
     s.close()
     rng = np.random.default_rng(73)
     b2 = np.stack([b, O.gaussian_spinor(rng, V).ravel()])
-    bsolver = BatchedWilsonSolver(dims, 2, KAPPA, tol=1e-10)
+    bsolver = BatchedWilsonSolver(dims, 2, KAPPA, tol=1e-10, outer_double_float=True)
     bsolver.set_gauge(ug)
     xt = torch.zeros(b2.size, dtype=torch.float64, device="cuda")
     stats = bsolver.solve(torch.from_numpy(b2.ravel()).cuda(), xt)
