@@ -212,7 +212,9 @@ int gbds_op_get_site_order(gbds_op op, int *zblock);
  * formats 2 the whole hop in packed FP32x2 (8, 16, 32 rhs), 3 the same with
  * two rhs per thread, for the 16-bit formats 4 (3 with cp.async prefetching)
  * and, for 16-bit formats with 16 or 32 rhs, the tensor-core kernel
- * (gbds_op_set_tensor_cores).  Synchronises `stream`. */
+ * (gbds_op_set_tensor_cores); for a CUDA-core pick it then times the site
+ * order (gbds_op_set_site_order): the natural order and z slabs of Lz/8
+ * planes and up.  Synchronises `stream`. */
 int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, void *res, void *stream);
 
 /* Number of kernels this library has launched in this process (all kinds). */

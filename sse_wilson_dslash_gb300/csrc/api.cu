@@ -318,8 +318,9 @@ extern "C" int gbds_op_num_variants(gbds_op op) {
 
 namespace {
 std::mutex g_tune_mutex;
-// (dims, nd, prec, recon, nrhs, format) -> (block, variant, tensor cores)
-std::map<std::array<int, 9>, std::array<int, 3>> g_tune_cache;
+// (dims, nd, prec, recon, nrhs, format) -> (block, variant, tensor cores,
+// z slab of the site order)
+std::map<std::array<int, 9>, std::array<int, 4>> g_tune_cache;
 }  // namespace
 
 static bool tc_eligible(gbds_op op) {
@@ -343,6 +344,7 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
         if (it != g_tune_cache.end()) {
             op->block = it->second[0];
             op->variant = it->second[1];
+            op->g.zblock = (short)it->second[3];
             return it->second[2] ? gbds_op_set_tensor_cores(op, 1) : gbds_op_set_tensor_cores(op, 0);
         }
     }
@@ -388,16 +390,42 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
         cudaEventElapsedTime(&ms, e0, e1);
         if (ms < best) { best = ms; pick = c; }
     }
+    if (e == cudaSuccess && rc == GBDS_SUCCESS) {
+        op->block = pick[0];
+        op->variant = pick[1];
+        rc = gbds_op_set_tensor_cores(op, pick[2]);
+    }
+    // the site order of the multi-RHS CUDA-core kernels: the natural order
+    // and z slabs of Lz/8 planes and up (divisors of Lz), for the kernel
+    // picked above
+    int zpick = op->g.zblock;
+    if (e == cudaSuccess && rc == GBDS_SUCCESS && generic(op) && !op->tensor_cores) {
+        const int Lz = op->g.L[2];
+        std::vector<int> zc = {0};
+        for (int b = 2; b < Lz && b < 32768; b++)
+            if (Lz % b == 0 && 8 * b >= Lz) zc.push_back(b);
+        float zbest = 1e30f;
+        for (int zb : zc) {
+            op->g.zblock = (short)zb;
+            rc = gbds_op_dslash(op, gauge, psi, res, 1, 0, stream);  // warm-up
+            if (rc != GBDS_SUCCESS) break;
+            cudaEventRecord(e0, s);
+            for (int r = 0; r < reps; r++) gbds_op_dslash(op, gauge, psi, res, (r & 1) ? -1 : 1, 0, stream);
+            cudaEventRecord(e1, s);
+            e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) break;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < zbest) { zbest = ms; zpick = zb; }
+        }
+        op->g.zblock = (short)zpick;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_error(e, "autotune");
     if (rc != GBDS_SUCCESS) return rc;
-    op->block = pick[0];
-    op->variant = pick[1];
-    rc = gbds_op_set_tensor_cores(op, pick[2]);
-    if (rc != GBDS_SUCCESS) return rc;
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    g_tune_cache[key] = pick;
+    g_tune_cache[key] = {pick[0], pick[1], pick[2], zpick};
     return GBDS_SUCCESS;
 }
 

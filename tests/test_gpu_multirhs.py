@@ -135,8 +135,10 @@ def test_tensor_cores_need_16bit_and_16_or_32_rhs():
 @pytest.mark.parametrize("fmt", ["bf16", "f16", "f32_pairs"])
 def test_autotune_chooses_between_cuda_and_tensor_cores(fmt):
     """The autotuner times the CUDA-core variants (and, for 16-bit storage,
-    the tensor-core kernel) for a 32-rhs operator; the pick (cached) gives the
-    same answer as the oracle."""
+    the tensor-core kernel) for a 32-rhs operator, then for a CUDA-core pick
+    the site order (natural, or z slabs of Lz/8 planes and up: here 0, 2 or
+    4); the pick (cached) gives the same answer as the oracle, and a second
+    operator of the same shape takes the cached site order."""
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
     dims, nrhs = (8, 8, 8, 8), 32
@@ -149,6 +151,7 @@ def test_autotune_chooses_between_cuda_and_tensor_cores(fmt):
     gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
     src = op.pack_spinor(torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda(), 0)
     op.autotune(gauge, src, op.new_spinor())
+    assert op.site_order() in (0, 2, 4)
     out = op.apply(gauge, src, 1, 0)
     op.check()
     res = torch.zeros(nrhs * V * 24, dtype=torch.float32, device="cuda")
@@ -158,6 +161,10 @@ def test_autotune_chooses_between_cuda_and_tensor_cores(fmt):
     for r in range(0, nrhs, 7):
         ref = O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), 1, 0)
         assert O.site_rel_err(got[r], ref, ts) <= TOL_TC.get(fmt, TOL[fmt])
+    again = DslashOperator(dims, nd=4, prec=32, recon=18, nrhs=nrhs, spinor_format=fmt)
+    again.autotune(gauge, src, again.new_spinor())  # from the cache
+    assert again.tuning() == op.tuning() and again.site_order() == op.site_order()
+    again.close()
     op.close()
 
 
