@@ -176,14 +176,14 @@ int gbds_op_dslash(gbds_op op, const void *gauge, const void *psi, void *res,
  * uncapped; 1.. = variants that cap registers for more resident warps, which
  * launch 128-thread blocks.  Several rhs or 16-bit storage: 0 = the plain
  * multi-RHS kernel, 1 = the packed FP32x2 form (8, 16, 32 rhs; the block
- * size is fixed at 128), and for the 16-bit and FP32-pair formats 2 =
- * projection, multiply and reconstruction all in packed FP32x2 (8, 16, 32
- * rhs; 128-thread blocks), 3 = variant 2 with two rhs per thread, which
- * share each staged link (the default from 16 rhs on for FP32 pairs), and
- * for the 16-bit formats 4 = variant 3 with each thread's neighbour spinors
- * prefetched two hops ahead by cp.async into shared memory (their default
- * from 16 rhs on).  Variants 1 to 4 run the plain
- * kernel for other counts of rhs (variant 4 on FP32 pairs runs variant 3).
+ * size is fixed at 128), 2 = projection, multiply and reconstruction all in
+ * packed FP32x2 (8, 16, 32 rhs; 128-thread blocks; every storage format),
+ * 3 = variant 2 with two rhs per thread, which share each staged link (the
+ * default from 16 rhs on for both FP32 layouts), and for the 16-bit formats
+ * 4 = variant 3 with each thread's neighbour spinors prefetched two hops
+ * ahead by cp.async into shared memory (their default from 16 rhs on).
+ * Variants 1 to 4 run the plain kernel for other counts of rhs (variant 4 on
+ * the FP32 formats runs variant 3).
  * gbds_op_num_variants gives the count.  Used by the autotuner. */
 int gbds_op_set_tuning(gbds_op op, int threads, int variant);
 int gbds_op_get_tuning(gbds_op op, int *threads, int *variant);

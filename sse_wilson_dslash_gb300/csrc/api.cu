@@ -147,17 +147,15 @@ extern "C" int gbds_op_create_ex(gbds_op *op, const int dims[4], int nd, int pre
     o->format = format;
     // Single rhs: the register-cap variant (see above).  Several rhs or
     // another format: variant 0 = the plain multi-RHS kernel, 1 = its packed
-    // FP32x2 colour multiply, 2 = the whole hop packed (16-bit and FP32-pair
-    // storage); from 16 rhs on (at 24^3x48) 2 is fastest where it exists and
-    // 1 for FP32 (autotune chooses per shape).
+    // FP32x2 colour multiply, 2 = the whole hop packed, 3 = the same with two
+    // rhs a thread, 4 = 3 with cp.async prefetching (16-bit storage);
+    // autotune chooses per shape.
     const bool gen = nrhs > 1 || (format != GBDS_SPINOR_NATIVE && format != GBDS_SPINOR_DOUBLE_FLOAT);
     // from 16 rhs on: for 16-bit storage the fully packed kernel with two rhs
-    // a thread and cp.async prefetching (variant 4), for FP32 pairs the same
-    // without prefetching (3), for FP32 the packed multiply (1)
-    const int gen_variant = nrhs >= 16 ? (format == GBDS_SPINOR_BF16 || format == GBDS_SPINOR_F16_NORM
-                                              ? 4
-                                              : (format == GBDS_SPINOR_F32_PAIRS ? 3 : 1))
-                                       : 0;
+    // a thread and cp.async prefetching (variant 4), for both FP32 layouts
+    // the same without prefetching (3)
+    const int gen_variant =
+        nrhs >= 16 ? (format == GBDS_SPINOR_BF16 || format == GBDS_SPINOR_F16_NORM ? 4 : 3) : 0;
     o->variant = gen ? gen_variant : ((prec == 32 && recon == 18) ? 1 : 0);
     if (gen) o->g.zblock = gen_zblock(g, nrhs, format, recon);
     o->tensor_cores = 0;
@@ -312,7 +310,7 @@ extern "C" int gbds_op_num_variants(gbds_op op) {
     if (!op) return 0;
     // 2: the fully packed kernel; 3: the same, two rhs a thread; 4: 3 with
     // cp.async prefetching (16-bit storage)
-    if (generic(op)) return op->format != GBDS_SPINOR_NATIVE ? 5 : 2;
+    if (generic(op)) return 5;
     return double_float(op) ? dslash_variants_df() : dslash_variants(op->prec);
 }
 
@@ -353,10 +351,10 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
     if (generic(op)) {
         cand = {{op->block, 0, 0}};
         if (v2ok) cand.push_back({op->block, 1, 0});
-        if (v2ok && op->format != GBDS_SPINOR_NATIVE) {
+        if (v2ok) {
             cand.push_back({op->block, 2, 0});
             cand.push_back({op->block, 3, 0});
-            if (op->format != GBDS_SPINOR_F32_PAIRS) cand.push_back({op->block, 4, 0});
+            if (op->format == GBDS_SPINOR_BF16 || op->format == GBDS_SPINOR_F16_NORM) cand.push_back({op->block, 4, 0});
         }
         if (tc_eligible(op)) cand.push_back({op->block, 0, 1});
     } else {

@@ -492,8 +492,19 @@ struct CPart {
 // the scale (the norm of half + norm, else 1)
 template <int FMT>
 __device__ __forceinline__ float load_reals(const char *base, size_t cs, size_t i, float (&v)[24]) {
-    static_assert(FMT == kFmtF32Pairs || FMT == kFmtBF16 || FMT == kFmtF16N, "pair-friendly formats");
-    if constexpr (FMT == kFmtF32Pairs) {
+    if constexpr (FMT == kFmtNative) {
+        // float4 k holds complex elements 2k and 2k + 1: the reals in order
+        const float4 *p = reinterpret_cast<const float4 *>(base);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const float4 q = __ldg(p + k * cs + i);
+            v[4 * k] = q.x;
+            v[4 * k + 1] = q.y;
+            v[4 * k + 2] = q.z;
+            v[4 * k + 3] = q.w;
+        }
+        return 1.f;
+    } else if constexpr (FMT == kFmtF32Pairs) {
         // the pair layout: no moves for the projection's operand pairs
         const float4 *p = reinterpret_cast<const float4 *>(base);
 #pragma unroll
@@ -824,7 +835,7 @@ __global__ void __launch_bounds__(128, 4) dslash_gen4_kernel(const GenArgs a) {
             const float sc = load_reals<FMT>(a.psi, a.cs, (size_t)(NB) * NRHS + r + q * H, v);         \
             packed_project<MU, SIG, SCALE>(v, sc, R[q], I[q]);                                         \
         }                                                                                              \
-        packed_mul_recon2<MU, SIG, LORD, FMT != kFmtF32Pairs>(sL[p][L], R, I, UR, UI, LR, LI);         \
+        packed_mul_recon2<MU, SIG, LORD, FMT == kFmtBF16 || FMT == kFmtF16N>(sL[p][L], R, I, UR, UI, LR, LI); \
     }
 #define GBDS_G4_DIR(MU, LORD)                                   \
     GBDS_G4_HOP(MU, LORD, n.f[MU], ISIGN, 2 * MU)               \

@@ -167,16 +167,16 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
     if (epi && (nrhs > 32 || (nrhs & (nrhs - 1)) != 0)) return cudaErrorInvalidValue;
     const bool packed_nrhs = nrhs == 8 || nrhs == 16 || nrhs == 32;
     const bool v2 = variant == 1 && packed_nrhs;
-    // variant 2 (fully packed: 16-bit and FP32-pair storage; its xpay
+    // variant 2 (fully packed, every format: the native FP32 layout holds
+    // the reals in order and the pairs are formed in registers; its xpay
     // epilogue serves the batched solver's FP32-pair fields); like variant 1,
     // it falls back to the plain kernel otherwise
-    const bool v3 = (variant >= 2 && variant <= 4) && packed_nrhs && FMT != kFmtNative &&
-                    (FMT == kFmtF32Pairs || !epi);
+    const bool v3 = (variant >= 2 && variant <= 4) && packed_nrhs && (FMT == kFmtF32Pairs || !epi);
     // variant 3: the fully packed kernel with two rhs per thread (no
     // epilogue; with one, variant 2 runs); variant 4: the same with cp.async
-    // prefetching (16-bit storage; variant 3 for FP32 spin pairs)
+    // prefetching (16-bit storage; variant 3 for the FP32 formats)
     const bool v5 = variant == 4 && packed_nrhs && (FMT == kFmtBF16 || FMT == kFmtF16N) && !epi;
-    const bool v4 = (variant == 3 || variant == 4) && packed_nrhs && FMT != kFmtNative && !epi;
+    const bool v4 = (variant == 3 || variant == 4) && packed_nrhs && !epi;
 #define GBDS_GEN(R, S)                                                   \
     do {                                                                 \
         if constexpr (FMT == kFmtBF16 || FMT == kFmtF16N) {              \
@@ -185,20 +185,18 @@ cudaError_t launch_gen_t(const Geom &g, int recon, int nrhs, const void *gauge, 
                 break;                                                   \
             }                                                            \
         }                                                                \
-        if constexpr (FMT != kFmtNative) {                               \
-            if (v4) {                                                    \
-                launch_gen4_nrhs<FMT, R, S>(a, nrhs, st);                \
-                break;                                                   \
+        if (v4) {                                                        \
+            launch_gen4_nrhs<FMT, R, S>(a, nrhs, st);                    \
+            break;                                                       \
+        }                                                                \
+        if (v3) {                                                        \
+            if constexpr (FMT == kFmtF32Pairs) {                         \
+                if (epi) launch_gen3_nrhs<FMT, R, S, 2>(a, nrhs, st);    \
+                else launch_gen3_nrhs<FMT, R, S, 0>(a, nrhs, st);        \
+            } else {                                                     \
+                launch_gen3_nrhs<FMT, R, S, 0>(a, nrhs, st);             \
             }                                                            \
-            if (v3) {                                                    \
-                if constexpr (FMT == kFmtF32Pairs) {                     \
-                    if (epi) launch_gen3_nrhs<FMT, R, S, 2>(a, nrhs, st); \
-                    else launch_gen3_nrhs<FMT, R, S, 0>(a, nrhs, st);    \
-                } else {                                                 \
-                    launch_gen3_nrhs<FMT, R, S, 0>(a, nrhs, st);         \
-                }                                                        \
-                break;                                                   \
-            }                                                            \
+            break;                                                       \
         }                                                                \
         if (v2 && epi) launch_gen2_nrhs<FMT, R, S, 2>(a, nrhs, st);      \
         else if (v2) launch_gen2_nrhs<FMT, R, S, 0>(a, nrhs, st);        \

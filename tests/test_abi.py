@@ -85,17 +85,17 @@ def test_spinor_formats_and_their_variants(libs):
     L = _lib.core()
     h = ctypes.c_void_p()
     d = (ctypes.c_int * 4)(4, 4, 4, 4)
-    for fmt, nbytes, nv in ((0, 96, 2), (1, 48, 5), (2, 52, 5), (3, 96, 5)):
+    for fmt, nbytes, nv in ((0, 96, 5), (1, 48, 5), (2, 52, 5), (3, 96, 5)):
         assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 32, 18, 32, fmt) == 0, L.gbds_get_last_error()
         V, Vh, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         assert L.gbds_op_geometry(h, ctypes.byref(V), ctypes.byref(Vh), ctypes.byref(st)) == 0
         assert L.gbds_op_spinor_bytes(h) == nbytes * st.value * 32
         assert L.gbds_op_num_variants(h) == nv
         # default from 16 rhs on: variant 4 (two rhs a thread, prefetched) for
-        # the 16-bit formats, 3 (two rhs a thread) for FP32 pairs, 1 for FP32
+        # the 16-bit formats, 3 (two rhs a thread) for both FP32 layouts
         blk, var = ctypes.c_int(), ctypes.c_int()
         assert L.gbds_op_get_tuning(h, ctypes.byref(blk), ctypes.byref(var)) == 0
-        assert var.value == {0: 1, 1: 4, 2: 4, 3: 3}[fmt]
+        assert var.value == {0: 3, 1: 4, 2: 4, 3: 3}[fmt]
         if fmt in (0, 3):
             assert L.gbds_op_set_tensor_cores(h, 1) != 0
         L.gbds_op_destroy(h)

@@ -262,7 +262,7 @@ def _production_error(production, nrhs, fmt, variant=None, tc=False, zblock=-1):
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("fmt,variants", [("native", (0, 1)), ("f32_pairs", (1, 2, 3)), ("bf16", (0, 2, 3, 4)),
+@pytest.mark.parametrize("fmt,variants", [("native", (0, 1, 2, 3)), ("f32_pairs", (1, 2, 3)), ("bf16", (0, 2, 3, 4)),
                                           ("f16", (2, 3, 4))])
 @pytest.mark.parametrize("nrhs", [16, 32])
 def test_multi_rhs_24x24x24x48_every_rhs_against_oracle(production, nrhs, fmt, variants):
@@ -296,10 +296,10 @@ def test_packed_fp32x2_variant_matches_oracle(nrhs, fmt):
     rng = np.random.default_rng(300 + nrhs)
     u = O.random_gauge(rng, V)
     psis = [O.gaussian_spinor(rng, V) for _ in range(nrhs)]
-    variants = (1,) if fmt == "native" else (1, 2, 3, 4)
+    variants = (1, 2, 3, 4)
     for recon, variant in [(rc, v) for rc in (18, 12) for v in variants]:
         op = DslashOperator(dims, nd=4, prec=32, recon=recon, nrhs=nrhs, spinor_format=fmt)
-        assert op.num_variants == (2 if fmt == "native" else 5)
+        assert op.num_variants == 5
         op.set_tuning(0, variant)
         gauge = op.pack_gauge(torch.from_numpy(u.astype(np.float32).ravel()).cuda())
         packed = torch.from_numpy(np.stack(psis).astype(np.float32).ravel()).cuda()
@@ -315,7 +315,7 @@ def test_packed_fp32x2_variant_matches_oracle(nrhs, fmt):
         op.close()
 
 
-@pytest.mark.parametrize("fmt", ["bf16", "f16", "f32_pairs"])
+@pytest.mark.parametrize("fmt", ["bf16", "f16", "f32_pairs", "native"])
 @pytest.mark.parametrize("nrhs", [8, 16, 32])
 def test_packed_variants_partial_last_cta(nrhs, fmt):
     """6x2x2x10: 120 sites a checkerboard, not a multiple of the 4-32 sites a
@@ -363,7 +363,7 @@ def test_site_orders_match_oracle(fmt, nrhs):
     isign, cb = -1, 1
     ts = O.target_sites(4, dims, lol, cb)
     refs = [O.dslash_plain(4, dims, lol, u.astype(np.float32), _round(psis[r], fmt), isign, cb) for r in range(nrhs)]
-    variants = (0, 1) if fmt == "native" else (0, 1, 2, 3, 4)
+    variants = (0, 1, 2, 3, 4)
     for variant in variants:
         op = DslashOperator(dims, nd=4, prec=32, recon=12, nrhs=nrhs, spinor_format=fmt)
         op.set_tuning(0, variant)
