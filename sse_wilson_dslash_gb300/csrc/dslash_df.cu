@@ -1,6 +1,7 @@
 // Double-float instantiations of the fused Dslash kernel (dfloat.cuh): FP64
 // fields stored as (hi, lo) FP32 pairs and computed on the FP32 pipes, and
-// the FP64 <-> double-float conversions of whole fields.
+// the FP64 -> double-float conversion of whole fields (the way back is part
+// of the unpack kernels).
 #include "dslash_kernel.cuh"
 
 namespace gbds {
@@ -11,11 +12,6 @@ namespace {
 __global__ void f64_to_df_kernel(const double2 *in, float4 *out, size_t n) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = df_from_double2(in[i]);
-}
-
-__global__ void df_to_f64_kernel(const float4 *in, double2 *out, size_t n) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = df_to_double2(in[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -243,12 +239,5 @@ cudaError_t launch_f64_to_df(const void *in, void *out, size_t n, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_df_to_f64(const void *in, void *out, size_t n, cudaStream_t stream) {
-    if (n == 0) return cudaSuccess;
-    df_to_f64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(static_cast<const float4 *>(in),
-                                                                       static_cast<double2 *>(out), n);
-    count_launch();
-    return cudaGetLastError();
-}
 
 }  // namespace gbds

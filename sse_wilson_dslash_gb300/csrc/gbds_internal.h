@@ -57,9 +57,8 @@ cudaError_t launch_dslash_df(const Geom &g, int recon, const void *gauge, const 
                              int cb, int block, int variant, cudaStream_t stream);
 cudaError_t launch_dslash_xpay_df(const Geom &g, int recon, const void *gauge, const void *psi, const void *x,
                                   double coef, void *res, double *partials, int isign, int cb, cudaStream_t stream);
-// n complex elements FP64 <-> double-float; in place allowed
+// n complex elements FP64 -> double-float; in place allowed
 cudaError_t launch_f64_to_df(const void *in, void *out, size_t n, cudaStream_t stream);
-cudaError_t launch_df_to_f64(const void *in, void *out, size_t n, cudaStream_t stream);
 
 // site0: first caller site held by the packed buffer (0 for a full lattice).
 // df (prec 64): the internal field is double-float (dfloat.cuh).
