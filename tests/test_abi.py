@@ -99,6 +99,12 @@ def test_spinor_formats_and_their_variants(libs):
         if fmt in (0, 3):
             assert L.gbds_op_set_tensor_cores(h, 1) != 0
         L.gbds_op_destroy(h)
+    # 8 rhs: the plain kernel, except half + norm (the fully packed one)
+    for fmt, want in ((0, 0), (1, 0), (2, 2), (3, 0)):
+        assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 32, 18, 8, fmt) == 0
+        blk, var = ctypes.c_int(), ctypes.c_int()
+        assert L.gbds_op_get_tuning(h, ctypes.byref(blk), ctypes.byref(var)) == 0 and var.value == want, fmt
+        L.gbds_op_destroy(h)
     assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 32, 18, 4, 4) != 0
     # the non-native formats need prec 32 and nd 4
     assert L.gbds_op_create_ex(ctypes.byref(h), d, 4, 64, 18, 1, 3) != 0
