@@ -32,13 +32,15 @@ def slab(dims, world: int, rank: int):
     return (Lx, Ly, Lz, lt), rank * lt
 
 
-def exchange_faces(to_prev, to_next, from_prev, from_next, group=None):
+def exchange_faces(to_prev, to_next, from_prev, from_next, group=None, timeout=None):
     """Send ``to_prev`` to the previous rank (its ``from_next``) and
     ``to_next`` to the next rank (its ``from_prev``), periodic in the rank
     index; receive the neighbours' faces.  Blocks until the faces have
     arrived (for NCCL: until the current stream waits for them).  Without an
     initialised process group, or with one rank, the rank is its own
-    neighbour."""
+    neighbour.  A neighbour that left or never arrives makes the waits raise
+    (RuntimeError) after ``timeout`` (a datetime.timedelta; default: the
+    process group's timeout) instead of blocking for good."""
     import torch.distributed as dist
     world = dist.get_world_size(group) if dist.is_available() and dist.is_initialized() else 1
     if world == 1:
@@ -59,7 +61,10 @@ def exchange_faces(to_prev, to_next, from_prev, from_next, group=None):
            dist.P2POp(dist.irecv, from_next, nxt, group, TAG_TO_PREV),
            dist.P2POp(dist.irecv, from_prev, prev, group, TAG_TO_NEXT)]
     for r in dist.batch_isend_irecv(ops):
-        r.wait()
+        if timeout is None:
+            r.wait()
+        else:
+            r.wait(timeout)
 
 
 class SplitDslash:

@@ -72,6 +72,47 @@ def test_split_ranks_match_the_oracle(world, dims):
         assert err < 1e-13, (r, err)
 
 
+def _rank_leaves(rank, world, port, results):
+    """Rank 1 leaves between steps (it never posts its half of the
+    exchange); rank 0's exchange must raise within the bounded wait."""
+    import datetime
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=20))
+    try:
+        from sse_wilson_dslash_gb300.halo import exchange_faces
+        if rank == 1:
+            results[rank] = "left"
+            return
+        faces = [torch.zeros(96, dtype=torch.float64) for _ in range(4)]
+        try:
+            exchange_faces(*faces, timeout=datetime.timedelta(seconds=3))
+            results[rank] = "completed"
+        except RuntimeError:
+            results[rank] = "raised"
+    finally:
+        dist.destroy_process_group()
+
+
+def test_a_rank_that_leaves_makes_the_exchange_raise():
+    """The failure is made on the host, as the split-t path's failure tests
+    are: one gloo rank leaves before the face exchange; the other's
+    exchange_faces raises RuntimeError within its bounded wait and the
+    process ends normally (no hang, no abort)."""
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    results = ctx.Manager().dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_leaves, args=(r, 2, port, results)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert results[1] == "left"
+    assert results[0] == "raised"
+
+
 def test_slab_partition_rules():
     from sse_wilson_dslash_gb300.halo import slab
     assert slab((8, 8, 8, 16), 4, 3) == ((8, 8, 8, 4), 12)
