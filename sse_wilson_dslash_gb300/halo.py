@@ -74,10 +74,12 @@ class SplitDslash:
     slab's local dims): pack with ``op.pack_gauge`` / ``op.pack_spinor`` from
     the slab's part of the packed arrays (local QDP++ cb2 order)."""
 
-    def __init__(self, global_dims, prec: int = 32, recon: int = 18, group=None, device=None):
+    def __init__(self, global_dims, prec: int = 32, recon: int = 18, group=None, device=None, timeout=None):
+        """timeout: bound on the face exchange's waits (exchange_faces)."""
         import torch.distributed as dist
         from .device import DslashOperator
         self.group = group
+        self.timeout = timeout
         self.world = dist.get_world_size(group) if dist.is_available() and dist.is_initialized() else 1
         self.rank = dist.get_rank(group) if self.world > 1 else 0
         self.global_dims = tuple(int(v) for v in global_dims)
@@ -98,14 +100,14 @@ class SplitDslash:
         stream = torch.cuda.current_stream(op.device)
         op.pack_faces(gauge, psi, isign, cb, self.to_prev, self.to_next, stream=stream)
         if not overlap:
-            exchange_faces(self.to_prev, self.to_next, self.from_prev, self.from_next, self.group)
+            exchange_faces(self.to_prev, self.to_next, self.from_prev, self.from_next, self.group, self.timeout)
             return op.apply_halo(gauge, psi, self.from_prev, self.from_next, isign, cb, out=out, part="all",
                                  stream=stream)
         if self._comm is None:
             self._comm = torch.cuda.Stream(op.device)
         self._comm.wait_stream(stream)
         with torch.cuda.stream(self._comm):
-            exchange_faces(self.to_prev, self.to_next, self.from_prev, self.from_next, self.group)
+            exchange_faces(self.to_prev, self.to_next, self.from_prev, self.from_next, self.group, self.timeout)
         op.apply_halo(gauge, psi, None, None, isign, cb, out=out, part="interior", stream=stream)
         stream.wait_stream(self._comm)
         return op.apply_halo(gauge, psi, self.from_prev, self.from_next, isign, cb, out=out, part="boundary",
