@@ -8,6 +8,8 @@ the same inputs, per site ||got - ref|| / ||ref|| <= 1e-6 (FP32) and 1e-13
   lib/sse_su3dslash_64bit_scalar.c:150-170);
 * 3D 24^3x48 in the cb3d site order: the same combinations
   (lib/sse_su3dslash_32bit_scalar_3d.c:150-359);
+* the FP64 operator in double-float arithmetic (GBDS_SPINOR_DOUBLE_FLOAT) on
+  both, at the FP64 tolerance;
 * the drop-in C ABI (sse_su3dslash_wilson of libgbdslash32.so / 64.so) on
   32^3x64 with the QDP++ cb2 callbacks, kernels reading the host arrays in
   place and staged through copies; the source checkerboard of res is left
@@ -42,10 +44,10 @@ def _inputs(dims, prec, seed):
     return u.cpu().numpy(), psi.cpu().numpy()
 
 
-def _device_operator_check(nd, dims, prec, recon, seed):
+def _device_operator_check(nd, dims, prec, recon, seed, fmt="native"):
     import torch
     from sse_wilson_dslash_gb300.device import DslashOperator
-    op = DslashOperator(dims, nd=nd, prec=prec, recon=recon)
+    op = DslashOperator(dims, nd=nd, prec=prec, recon=recon, spinor_format=fmt)
     assert op.canonical
     u, psi = _inputs(dims, prec, seed)
     V = op.volume
@@ -65,7 +67,7 @@ def _device_operator_check(nd, dims, prec, recon, seed):
         assert not np.any(got.reshape(V, 24)[O.target_sites(nd, dims, lol, 1 - cb)])
     op.close()
     for k, e in errs.items():
-        assert e <= SITE_TOL[prec], (nd, dims, prec, recon, k, e)
+        assert e <= SITE_TOL[prec], (nd, dims, prec, recon, fmt, k, e)
     return errs
 
 
@@ -73,6 +75,15 @@ def _device_operator_check(nd, dims, prec, recon, seed):
 @pytest.mark.parametrize("prec", [32, 64])
 def test_4d_32x32x32x64_every_site_every_combination(prec, recon):
     _device_operator_check(4, DIMS_4D, prec, recon, seed=40 + prec + recon)
+
+
+@pytest.mark.parametrize("nd,dims", [(4, DIMS_4D), (3, DIMS_3D)])
+@pytest.mark.parametrize("recon", [18, 12])
+def test_double_float_at_production_size(nd, dims, recon):
+    """The FP64 operator in double-float arithmetic (GBDS_SPINOR_DOUBLE_FLOAT)
+    at the production sizes, every target site and combination against the
+    oracle at the FP64 tolerance (1e-13)."""
+    _device_operator_check(nd, dims, 64, recon, seed=70 + nd + recon, fmt="double_float")
 
 
 @pytest.mark.parametrize("recon", [18, 12])
