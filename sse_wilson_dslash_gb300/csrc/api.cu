@@ -397,7 +397,8 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
     // the site order of the multi-RHS CUDA-core kernels: the natural order
     // and z slabs of Lz/8 planes and up (divisors of Lz), for the kernel
     // picked above
-    int zpick = op->g.zblock;
+    const short zstart = op->g.zblock;
+    int zpick = zstart;
     if (e == cudaSuccess && rc == GBDS_SUCCESS && generic(op) && !op->tensor_cores) {
         const int Lz = op->g.L[2];
         std::vector<int> zc = {0};
@@ -417,7 +418,8 @@ extern "C" int gbds_op_autotune(gbds_op op, const void *gauge, const void *psi, 
             cudaEventElapsedTime(&ms, e0, e1);
             if (ms < zbest) { zbest = ms; zpick = zb; }
         }
-        op->g.zblock = (short)zpick;
+        // on an error the operator keeps the order it came with
+        op->g.zblock = (e == cudaSuccess && rc == GBDS_SUCCESS) ? (short)zpick : zstart;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
