@@ -109,7 +109,7 @@ int gbds_op_destroy(gbds_op op);
  * have specialised kernels) and a spinor storage format.
  * GBDS_SPINOR_DOUBLE_FLOAT needs prec 64 and nrhs 1 (nd 3 or 4; fields of
  * FP64 size; not for the force or the split-t entry points).  nrhs > 1 or
- * another format other than GBDS_SPINOR_NATIVE needs prec 32 and nd 4;
+ * any other format except GBDS_SPINOR_NATIVE needs prec 32 and nd 4;
  * arithmetic is FP32.  A field then holds nrhs spinors per
  * site, element (k, h, r) at k*stride*nrhs + h*nrhs + r (k: 16-byte component,
  * h: site, r: right-hand side), half formats followed by one float norm per
@@ -196,8 +196,9 @@ int gbds_op_num_variants(gbds_op op);
  * source spinor's eight reads stay within about 2 B planes and hit L2; 0 or
  * Lz: the natural checkerboard order; -1: the default, the largest slab whose
  * reuse span fits in a fixed share of L2 (natural order when the whole
- * lattice's span fits).  Results are the same in every order up to the
- * per-block partial sums' order.  Storage layouts do not change.
+ * lattice's span fits); gbds_op_autotune times the orders.  Outputs are
+ * bit-identical in every order; only the grouping of per-block partial sums
+ * (the solver epilogues' norms) follows it.  Storage layouts do not change.
  * get: the slab in use (0 = natural order). */
 int gbds_op_set_site_order(gbds_op op, int zblock);
 int gbds_op_get_site_order(gbds_op op, int *zblock);
@@ -208,9 +209,9 @@ int gbds_op_get_site_order(gbds_op op, int *zblock);
  * for the same shape takes the cached choice without timing.  Operators with
  * several right-hand sides (or 16-bit storage) have these candidates: 0 the
  * plain multi-RHS kernel, 1 the colour multiply in packed FP32x2 arithmetic
- * on links staged per CTA (8, 16 or 32 rhs), for the 16-bit and FP32-pair
- * formats 2 the whole hop in packed FP32x2 (8, 16, 32 rhs), 3 the same with
- * two rhs per thread, for the 16-bit formats 4 (3 with cp.async prefetching)
+ * on links staged per CTA (8, 16 or 32 rhs), 2 the whole hop in packed
+ * FP32x2 (8, 16, 32 rhs), 3 the same with two rhs per thread, for the 16-bit
+ * formats 4 (3 with cp.async prefetching)
  * and, for 16-bit formats with 16 or 32 rhs, the tensor-core kernel
  * (gbds_op_set_tensor_cores); for a CUDA-core pick it then times the site
  * order (gbds_op_set_site_order): the natural order and z slabs of Lz/8
