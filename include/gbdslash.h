@@ -383,11 +383,13 @@ typedef struct gbds_solver_stats {
     int cycles;           /* defect-correction cycles (1 for FP64 CG) */
     int converged;        /* residual <= tol */
     double residual;      /* |c - A x| / |c| = |M^+ (b - M x)| / |M^+ b|: for the
-                             mixed-precision solves b - M x is formed in FP64
-                             and M^+ applied in FP32 (FP32 relative accuracy of
-                             the residual's own size); FP64 throughout for the
-                             FP64 CG and the normal-equation solve */
-    double true_residual; /* |b - M x| / |b|, FP64 */
+                             mixed-precision solves b - M x is formed on FP64
+                             fields (the FP64 operator, or the double-float one
+                             with outer_double_float) and M^+ applied in FP32
+                             (FP32 relative accuracy of the residual's own
+                             size); FP64 throughout for the FP64 CG and the
+                             normal-equation solve */
+    double true_residual; /* |b - M x| / |b| on FP64 fields, as above */
     double seconds;       /* wall time of the solve, including its syncs */
 } gbds_solver_stats;
 

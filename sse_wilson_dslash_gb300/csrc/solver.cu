@@ -792,8 +792,8 @@ static int solve_mixed(gbds_solver s, const double *b_packed, double *x_packed, 
         total += it;
         out.cycles++;
         if (e != cudaSuccess) break;
-        // x += |c| e (the correction A^-1 M^+ r);  r = b - M x (FP64 fields,
-        // the operator in double-float)
+        // x += |c| e (the correction A^-1 M^+ r);  r = b - M x on FP64 fields
+        // (the FP64 operator, or the double-float one with outer_double_float)
         promote_scaled<<<nb, kThreads, 0, st>>>(static_cast<const float4 *>(s->e32), std::sqrt(n2),
                                                 static_cast<double2 *>(s->x64), g.Vh, g.stride);
         count_launch();
