@@ -543,8 +543,8 @@ __device__ __forceinline__ float load_reals(const char *base, size_t cs, size_t 
 // One hop: project v (scaled by nrm for half + norm), multiply by the staged
 // M, add into the upper pairs U and the lower pairs L (order LORD: 0 =
 // (acc2, acc3), 1 = (acc3, acc2)).
-template <int MU, int SIG, int LORD, bool SCALE>
-__device__ __forceinline__ void packed_hop(const float (&v)[24], float nrm, const float4 *M, float2 (&UR)[3],
+template <int MU, int SIG, int LORD, bool SCALE, typename SPLAT>
+__device__ __forceinline__ void packed_hop(const float (&v)[24], float nrm, const SPLAT *M, float2 (&UR)[3],
                                            float2 (&UI)[3], float2 (&LR)[3], float2 (&LI)[3]) {
     using P = Proj<MU>;
     constexpr int f = SIG > 0 ? 0 : 1;
@@ -572,8 +572,16 @@ __device__ __forceinline__ void packed_hop(const float (&v)[24], float nrm, cons
         float2 ar = make_float2(0.f, 0.f), br = make_float2(0.f, 0.f), ai = make_float2(0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            const float4 m = M[i * 3 + j];
-            const float2 mr = make_float2(m.x, m.y), mi = make_float2(m.z, m.w);
+            float2 mr, mi;
+            if constexpr (std::is_same_v<SPLAT, float4>) {
+                const float4 m = M[i * 3 + j];
+                mr = make_float2(m.x, m.y);
+                mi = make_float2(m.z, m.w);
+            } else {
+                const float2 m = M[i * 3 + j];  // (Mr, Mi): the pairs formed in registers
+                mr = make_float2(m.x, m.x);
+                mi = make_float2(m.y, m.y);
+            }
             ar = __ffma2_rn(mr, R[j], ar);
             br = __ffma2_rn(mi, I[j], br);
             ai = __ffma2_rn(mr, I[j], ai);
@@ -596,7 +604,7 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
     pdl_wait_prev();
     constexpr int P = 128 / NRHS;  // sites per CTA
     constexpr bool SCALE = FMT == kFmtF16N;
-    __shared__ float4 sL[P][8][9];
+    __shared__ float2 sL[P][8][9];  // (Mr, Mi) splats
     const int t = threadIdx.x;
     const int p = t / NRHS, r = t % NRHS;
     const int h = gen_site(a.g, blockIdx.x * P + p);
@@ -631,7 +639,7 @@ __global__ void __launch_bounds__(128, 5) dslash_gen3_kernel(const GenArgs a) {
                 // forward: M_ij = U_ij; backward: M_ij = conj(U_ji)
                 const float mr = bwd ? U[j][i].r : U[i][j].r;
                 const float mi = bwd ? -U[j][i].i : U[i][j].i;
-                sL[p][r][i * 3 + j] = make_float4(mr, mr, mi, mi);
+                sL[p][r][i * 3 + j] = make_float2(mr, mi);
             }
     }
     __syncthreads();
@@ -744,8 +752,11 @@ __device__ __forceinline__ void packed_project(const float (&v)[24], float nrm, 
 // FOLD: the real part's chain takes -Mi I directly (one FFMA2 fewer per
 // output colour; measured faster for 16-bit storage, while FP32 spin pairs
 // spill with it at the 128-register cap).
-template <int MU, int SIG, int LORD, bool FOLD>
-__device__ __forceinline__ void packed_mul_recon2(const float4 *M, const float2 (&R)[2][3], const float2 (&I)[2][3],
+// M: the staged splats of the link, (Mr, Mr, Mi, Mi) as float4 or (Mr, Mi)
+// as float2 (half the shared-memory traffic; the pairs are formed in
+// registers)
+template <int MU, int SIG, int LORD, bool FOLD, typename SPLAT>
+__device__ __forceinline__ void packed_mul_recon2(const SPLAT *M, const float2 (&R)[2][3], const float2 (&I)[2][3],
                                                   float2 (&UR)[2][3], float2 (&UI)[2][3], float2 (&LR)[2][3],
                                                   float2 (&LI)[2][3]) {
     using P = Proj<MU>;
@@ -763,12 +774,20 @@ __device__ __forceinline__ void packed_mul_recon2(const float4 *M, const float2 
         for (int q = 0; q < 2; q++) ar[q] = br[q] = ai[q] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            const float4 m = M[i * 3 + j];
-            const float2 mr = make_float2(m.x, m.y), mi = make_float2(m.z, m.w);
+            float2 mr, mi;
+            if constexpr (std::is_same_v<SPLAT, float4>) {
+                const float4 m = M[i * 3 + j];
+                mr = make_float2(m.x, m.y);
+                mi = make_float2(m.z, m.w);
+            } else {
+                const float2 m = M[i * 3 + j];
+                mr = make_float2(m.x, m.x);
+                mi = make_float2(m.y, m.y);
+            }
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 ar[q] = __ffma2_rn(mr, R[q][j], ar[q]);
-                if constexpr (FOLD) ar[q] = __ffma2_rn(make_float2(-m.z, -m.w), I[q][j], ar[q]);
+                if constexpr (FOLD) ar[q] = __ffma2_rn(make_float2(-mi.x, -mi.y), I[q][j], ar[q]);
                 else br[q] = __ffma2_rn(mi, I[q][j], br[q]);
                 ai[q] = __ffma2_rn(mr, I[q][j], ai[q]);
                 ai[q] = __ffma2_rn(mi, R[q][j], ai[q]);
@@ -793,7 +812,7 @@ __global__ void __launch_bounds__(128, 4) dslash_gen4_kernel(const GenArgs a) {
     constexpr int H = NRHS / 2;    // threads per site
     constexpr int P = 128 / H;     // sites per CTA
     constexpr bool SCALE = FMT == kFmtF16N;
-    __shared__ float4 sL[P][8][9];
+    __shared__ float2 sL[P][8][9];  // (Mr, Mi) splats
     const int t = threadIdx.x;
     const int p = t / H, r = t % H;  // this thread: rhs r and r + H of site p
     const int h = gen_site(a.g, blockIdx.x * P + p);
@@ -817,7 +836,7 @@ __global__ void __launch_bounds__(128, 4) dslash_gen4_kernel(const GenArgs a) {
                 // forward: M_ij = U_ij; backward: M_ij = conj(U_ji)
                 const float mr = bwd ? U[j][i].r : U[i][j].r;
                 const float mi = bwd ? -U[j][i].i : U[i][j].i;
-                sL[p][l][i * 3 + j] = make_float4(mr, mr, mi, mi);
+                sL[p][l][i * 3 + j] = make_float2(mr, mi);
             }
     }
     __syncthreads();
@@ -897,7 +916,7 @@ struct G5Smem {
     // 32 rhs, 24^3x48: 0.455 against 0.437 ms)
     static constexpr int SLOTS = 3;
     static constexpr int MINB = 4;
-    static constexpr size_t link_bytes = (size_t)P * 8 * 9 * 16;
+    static constexpr size_t link_bytes = (size_t)P * 8 * 9 * 8;  // (Mr, Mi) float2 splats
     static constexpr size_t ring_bytes = (size_t)SLOTS * 2 * 3 * 128 * 16;
     static constexpr size_t norm_bytes = FMT == kFmtF16N ? (size_t)SLOTS * 2 * 128 * 4 : 0;
     static constexpr size_t bytes = link_bytes + ring_bytes + norm_bytes;
@@ -954,7 +973,7 @@ __global__ void __launch_bounds__(128, G5Smem<FMT, NRHS>::MINB) dslash_gen5_kern
     constexpr int P = SM::P;
     constexpr bool SCALE = FMT == kFmtF16N;
     extern __shared__ __align__(16) unsigned char g5s[];
-    float4 (*sL)[8][9] = reinterpret_cast<float4 (*)[8][9]>(g5s);
+    float2 (*sL)[8][9] = reinterpret_cast<float2 (*)[8][9]>(g5s);
     uint4 *ring = reinterpret_cast<uint4 *>(g5s + SM::link_bytes);
     float *rnorm = reinterpret_cast<float *>(g5s + SM::link_bytes + SM::ring_bytes);
     const int t = threadIdx.x;
@@ -985,7 +1004,7 @@ __global__ void __launch_bounds__(128, G5Smem<FMT, NRHS>::MINB) dslash_gen5_kern
             for (int j = 0; j < 3; j++) {
                 const float mr = bwd ? U[j][i].r : U[i][j].r;
                 const float mi = bwd ? -U[j][i].i : U[i][j].i;
-                sL[p][l][i * 3 + j] = make_float4(mr, mr, mi, mi);
+                sL[p][l][i * 3 + j] = make_float2(mr, mi);
             }
     }
     __syncthreads();
