@@ -306,6 +306,14 @@ def test_site_order_validation_and_defaults(libs):
         create((24, 24, 24, 48), nrhs, fmt)
         assert order() == want, (nrhs, fmt)
         L.gbds_op_destroy(h)
+    # a z extent beyond the slab field's 16 bits: 2-site planes of 32 rhs
+    # (6528 B a site) fit 2451 planes in the budget -> 2048, the largest
+    # divisor of 65536 below that; a slab of 32768 planes is refused
+    create((2, 2, 65536, 2), 32, 3)
+    assert order() == 2048
+    assert L.gbds_op_set_site_order(h, 32768) == 5 and order() == 2048
+    assert L.gbds_op_set_site_order(h, 65536) == 0 and order() == 0
+    L.gbds_op_destroy(h)
 
 
 def test_double_float_format_validation(libs):
